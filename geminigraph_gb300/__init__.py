@@ -1,0 +1,274 @@
+"""GB300-native edge-processing engine for Gemini graphs (Python front end).
+
+A thin ctypes layer over the C ABI in include/gemini_gb300.h
+(libgemini_gb300.so, built in-tree by geminigraph_gb300/build.py).  There is
+no CPU fallback: if the library is missing or no GPU is present, calls raise.
+
+    g = Graph.load("graph.bin", vertices)            # Graph::load_directed
+    g = Graph.load("graph.bin", vertices, symmetric=True)
+    parent, stats = g.bfs(root)                      # toolkits/bfs.cpp
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgemini_gb300.so")
+
+GG_OK = 0
+STATUS = {1: "invalid argument", 2: "I/O error", 3: "vertex id out of range", 4: "CUDA error",
+          5: "out of memory", 6: "graph is unweighted", 7: "graph too large", 8: "capacity exceeded"}
+
+RMAT, GRID = 0, 1
+
+_lib = None
+
+
+class GeminiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Info(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_uint32), ("edges", ctypes.c_uint64), ("adj_entries", ctypes.c_uint64),
+                ("weighted", ctypes.c_int32), ("symmetric", ctypes.c_int32), ("transposed", ctypes.c_int32),
+                ("device", ctypes.c_int32), ("device_bytes", ctypes.c_uint64)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("trace_capacity", ctypes.c_int32), ("calls", ctypes.c_int32),
+                ("mode", ctypes.c_void_p), ("active_edges", ctypes.c_void_p), ("activated", ctypes.c_void_p),
+                ("active_edges_total", ctypes.c_uint64), ("device_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int32)]
+
+
+def library():
+    """Loads libgemini_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run python -c 'import __graft_entry__ as g; g.build()'")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    pg = ctypes.POINTER(vp)
+    sig = {
+        "gg_last_error": ([], ctypes.c_char_p),
+        "gg_graph_load": ([ctypes.c_char_p, u32, i32, i32, i32, pg], i32),
+        "gg_graph_from_records": ([vp, u64, u32, i32, i32, i32, pg], i32),
+        "gg_graph_from_device_records": ([vp, u64, u32, i32, i32, i32, pg], i32),
+        "gg_graph_generate": ([i32, u32, u32, u64, i32, i32, i32, pg], i32),
+        "gg_generate_count": ([i32, u32, u32], u64),
+        "gg_generate_records": ([i32, u32, u32, u64, i32, vp, i32], i32),
+        "gg_graph_free": ([vp], i32),
+        "gg_graph_info_get": ([vp, ctypes.POINTER(_Info)], i32),
+        "gg_graph_transpose": ([vp], i32),
+        "gg_graph_adjacency": ([vp, i32, vp, vp, vp, vp], i32),
+        "gg_bfs": ([vp, u32, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_pagerank": ([vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_pagerank_f32": ([vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_cc": ([vp, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_sssp": ([vp, u32, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_bc": ([vp, u32, vp, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_result_device_ptr": ([vp, i32], vp),
+        "gg_active_edges": ([vp, vp, ctypes.POINTER(u64)], i32),
+        "gg_is_sparse": ([u64, u64], i32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != GG_OK:
+        raise GeminiError(rc, library().gg_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class RunStats:
+    """Per-call trace of one toolkit run: mode (0 sparse, 1 dense),
+    active_edges and activated per process_edges call."""
+
+    def __init__(self, capacity=1 << 16):
+        self.mode = np.zeros(capacity, np.int32)
+        self.active_edges = np.zeros(capacity, np.uint64)
+        self.activated = np.zeros(capacity, np.uint64)
+        self.s = _Stats(capacity, 0, self.mode.ctypes.data, self.active_edges.ctypes.data,
+                        self.activated.ctypes.data, 0, 0.0, 0)
+
+    @property
+    def calls(self):
+        return self.s.calls
+
+    @property
+    def device_ms(self):
+        return self.s.device_ms
+
+    @property
+    def active_edges_total(self):
+        return int(self.s.active_edges_total)
+
+    @property
+    def kernel_launches(self):
+        return self.s.kernel_launches
+
+    def rows(self):
+        n = min(self.s.calls, len(self.mode))
+        return [(int(self.mode[i]), int(self.active_edges[i]), int(self.activated[i])) for i in range(n)]
+
+
+def generate_records(kind, p1, p2, seed, weighted=False, threads=0):
+    """Host generator: the packed edge-list records of a seeded R-MAT
+    (kind=RMAT, p1=scale, p2=edge factor) or grid (kind=GRID, p1=side)."""
+    L = library()
+    n = int(L.gg_generate_count(kind, p1, p2))
+    unit = 12 if weighted else 8
+    buf = np.empty(n * unit, np.uint8)
+    _check(L.gg_generate_records(kind, p1, p2, seed, int(weighted), _ptr(buf), threads))
+    return buf
+
+
+class Graph:
+    """One graph resident on one GPU (Graph<EdgeData>, core/graph.hpp:91)."""
+
+    def __init__(self, handle):
+        self.h = handle
+        self._info = None
+
+    # -- construction -------------------------------------------------------
+    @classmethod
+    def load(cls, path, vertices, weighted=False, symmetric=False, device=0):
+        """Graph::load_directed / load_undirected_from_directed."""
+        h = ctypes.c_void_p()
+        _check(library().gg_graph_load(os.fsencode(path), vertices, int(weighted), int(symmetric), device,
+                                       ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_records(cls, records, vertices, weighted=False, symmetric=False, device=0):
+        buf = np.frombuffer(records, np.uint8) if isinstance(records, (bytes, bytearray)) else \
+            np.ascontiguousarray(records).view(np.uint8)
+        h = ctypes.c_void_p()
+        _check(library().gg_graph_from_records(_ptr(buf), buf.nbytes, vertices, int(weighted), int(symmetric),
+                                               device, ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_edges(cls, vertices, src, dst, w=None, symmetric=False, device=0):
+        n = len(src)
+        if w is None:
+            rec = np.empty(n, dtype=[("s", "<u4"), ("d", "<u4")])
+        else:
+            rec = np.empty(n, dtype=[("s", "<u4"), ("d", "<u4"), ("w", "<f4")])
+            rec["w"] = w
+        rec["s"] = src
+        rec["d"] = dst
+        return cls.from_records(rec, vertices, weighted=w is not None, symmetric=symmetric, device=device)
+
+    @classmethod
+    def generate(cls, kind, p1, p2, seed, weighted=False, symmetric=False, device=0):
+        h = ctypes.c_void_p()
+        _check(library().gg_graph_generate(kind, p1, p2, seed, int(weighted), int(symmetric), device,
+                                           ctypes.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self.h:
+            library().gg_graph_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- public fields ------------------------------------------------------
+    def info(self):
+        i = _Info()
+        _check(library().gg_graph_info_get(self.h, ctypes.byref(i)))
+        return {k: getattr(i, k) for k, _ in _Info._fields_}
+
+    @property
+    def vertices(self):
+        return self.info()["vertices"]
+
+    @property
+    def edges(self):
+        return self.info()["edges"]
+
+    def transpose(self):
+        _check(library().gg_graph_transpose(self.h))
+
+    def adjacency(self, incoming=False):
+        inf = self.info()
+        V, n = inf["vertices"], inf["adj_entries"]
+        off = np.zeros(V + 1, np.uint64)
+        nbr = np.zeros(max(n, 1), np.uint32)
+        w = np.zeros(max(n, 1), np.float32) if inf["weighted"] else None
+        deg = np.zeros(V, np.uint32)
+        _check(library().gg_graph_adjacency(self.h, int(incoming), _ptr(off), _ptr(nbr), _ptr(w), _ptr(deg)))
+        return off, nbr[:n], (None if w is None else w[:n]), deg
+
+    def out_degree(self):
+        return self.adjacency(False)[3]
+
+    def active_edges(self, bitmap64):
+        out = ctypes.c_uint64()
+        b = np.ascontiguousarray(bitmap64, np.uint64)
+        _check(library().gg_active_edges(self.h, _ptr(b), ctypes.byref(out)))
+        return int(out.value)
+
+    # -- toolkits -------------------------------------------------------------
+    def bfs(self, root, to_host=True):
+        st = RunStats()
+        parent = np.empty(self.vertices, np.uint32) if to_host else None
+        _check(library().gg_bfs(self.h, root, _ptr(parent), ctypes.byref(st.s)))
+        return parent, st
+
+    def pagerank(self, iterations, to_host=True, f32=False):
+        st = RunStats()
+        V = self.vertices
+        ranks = np.empty(V, np.float32 if f32 else np.float64) if to_host else None
+        deltas = np.zeros(max(iterations, 1), np.float64)
+        fn = library().gg_pagerank_f32 if f32 else library().gg_pagerank
+        _check(fn(self.h, iterations, _ptr(ranks), _ptr(deltas), ctypes.byref(st.s)))
+        return ranks, deltas[:iterations], st
+
+    def cc(self, to_host=True):
+        st = RunStats()
+        label = np.empty(self.vertices, np.uint32) if to_host else None
+        _check(library().gg_cc(self.h, _ptr(label), ctypes.byref(st.s)))
+        return label, st
+
+    def sssp(self, root, to_host=True):
+        st = RunStats()
+        dist = np.empty(self.vertices, np.float32) if to_host else None
+        _check(library().gg_sssp(self.h, root, _ptr(dist), ctypes.byref(st.s)))
+        return dist, st
+
+    def bc(self, root, to_host=True):
+        st = RunStats()
+        V = self.vertices
+        dep = np.empty(V, np.float64) if to_host else None
+        inv = np.empty(V, np.float64) if to_host else None
+        _check(library().gg_bc(self.h, root, _ptr(dep), _ptr(inv), ctypes.byref(st.s)))
+        return dep, inv, st
+
+
+def pick_roots(out_degree, count, seed):
+    """Seeded uniform draws of vertices with out-degree > 0 (BASELINE's
+    "non-isolated" roots)."""
+    rng = np.random.default_rng(seed)
+    cand = np.nonzero(np.asarray(out_degree) > 0)[0]
+    if len(cand) == 0:
+        raise ValueError("no vertex with out-degree > 0")
+    return [int(x) for x in cand[rng.integers(0, len(cand), count)]]

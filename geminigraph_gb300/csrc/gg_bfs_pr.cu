@@ -1,0 +1,287 @@
+// BFS (toolkits/bfs.cpp) and PageRank (toolkits/pagerank.cpp) on the
+// device engine, plus the process_vertices reduction of the switch.
+#include "gg_engine.cuh"
+
+namespace gg {
+
+constexpr uint32_t PULL_SMALL = 32;
+
+// ------------------------------------------------------------------ BFS
+// Sparse slot (bfs.cpp:49-59): claim unvisited dst with a CAS on its parent.
+struct BfsPush {
+  uint32_t *parent;
+  uint32_t V;
+  __device__ __forceinline__ bool push(uint32_t src, uint32_t, uint32_t dst, float) const {
+    if (*(volatile uint32_t *)(parent + dst) != V) return false;
+    return atomicCAS(parent + dst, V, src) == V;
+  }
+};
+
+__global__ void bfs_root(uint32_t *parent, uint32_t root, uint32_t *visited, uint32_t *active, uint32_t *q,
+                         const uint32_t *out_deg, Counters *ctr) {
+  parent[root] = root;
+  visited[root >> 5] |= 1u << (root & 31);
+  active[root >> 5] |= 1u << (root & 31);
+  q[0] = root;
+  ctr->edges = out_deg[root];
+  ctr->activated = 1;
+  ctr->qlen = 1;
+}
+
+static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_stats *st) {
+  if (root >= g->V) {
+    set_error("root %u >= vertices %u", root, g->V);
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  const uint32_t V = g->V;
+  const size_t words = bitmap_words32(V);
+  uint32_t *parent, *visited, *bm[2], *q[2];
+  GG_TRY(ws(g, WS_S0, V, &parent));
+  GG_TRY(ws(g, WS_BM0, words, &visited));
+  GG_TRY(ws(g, WS_BM1, words, &bm[0]));
+  GG_TRY(ws(g, WS_BM2, words, &bm[1]));
+  GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
+  GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
+  Launch L(g);
+  Trace tr(st, g);
+  cudaStream_t s = g->stream;
+  Counters *ctr = g->ws.ctr;
+  GG_TRY(timed_begin(g));
+  GG_CUDA(cudaMemsetAsync(visited, 0, words * 4, s));
+  GG_CUDA(cudaMemsetAsync(bm[0], 0, words * 4, s));
+  GG_TRY(counters_reset(g));
+  fill_kernel<uint32_t><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(parent, V, V);
+  bfs_root<<<1, 1, 0, s>>>(parent, root, visited, bm[0], q[0], g->out.deg, ctr);
+  L.launches += 2;
+  GG_CUDA(cudaGetLastError());
+  Counters c;
+  GG_TRY(counters_read(g, &c));
+  unsigned long long ae = c.edges;
+  uint32_t n = c.qlen;
+  int cur = 0;
+  while (n > 0) {
+    bool sparse = ae < g->E / 20;
+    tr.add(sparse ? 0 : 1, ae, 0);
+    int nx = cur ^ 1;
+    GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
+    GG_TRY(counters_reset(g));
+    ActOut a;
+    a.active_out = bm[nx];
+    a.visited = visited;
+    a.q_out = q[nx];
+    a.qlen = &ctr->qlen;
+    a.out_deg = g->out.deg;
+    if (sparse) {
+      if (ae > 0) {
+        unsigned long long *P;
+        GG_TRY(L.scan_queue_degrees(q[cur], n, g->out.deg, &P));
+        GG_TRY(tr.kbegin());
+        push_lb<BfsPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[cur], P, n, ae, g->out, BfsPush{parent, V}, a,
+                                                                    ctr);
+        GG_TRY(tr.kend());
+        L.launches += 1;
+      }
+    } else {
+      GG_TRY(tr.kbegin());
+      bfs_pull<<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL, bm[cur], parent, a, ctr);
+      GG_TRY(tr.kend());
+      L.launches += 1;
+    }
+    GG_CUDA(cudaGetLastError());
+    GG_TRY(counters_read(g, &c));
+    n = c.qlen;
+    ae = c.edges;
+    tr.set_activated(c.activated);
+    cur = nx;
+  }
+  GG_TRY(timed_end(g, st, L.launches));
+  GG_TRY(tr.collect());
+  if (parent_host) GG_CUDA(cudaMemcpy(parent_host, parent, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = parent;
+  g->result[1] = nullptr;
+  return GG_OK;
+}
+
+// ------------------------------------------------------------------ PageRank
+// toolkits/pagerank.cpp:26-129.  Active = all vertices, so every
+// process_edges call is dense (active_edges = edges >= edges/20); the pull
+// gathers curr over the CSC and the process_vertices update that follows it
+// (pagerank.cpp:77-97) is fused into the same kernel's epilogue.
+template <typename T>
+struct PrPull {
+  using Acc = T;
+  const T *curr;
+  T *next;
+  const uint32_t *out_deg;
+  int last;
+  __device__ __forceinline__ bool want(uint32_t) const { return true; }
+  __device__ __forceinline__ T identity(uint32_t) const { return T(0); }
+  __device__ __forceinline__ T identity_coop() const { return T(0); }
+  __device__ __forceinline__ T gather(const Dir &d, unsigned long long k) const { return curr[d.nbr[k]]; }
+  __device__ __forceinline__ T combine(T a, T b) const { return a + b; }
+  __device__ __forceinline__ T warp_combine(T x) const { return warp_sum(x); }
+  __device__ __forceinline__ bool finish(uint32_t v, T sum, uint32_t, Tally &t) const;
+};
+
+template <>
+__device__ __forceinline__ bool PrPull<double>::finish(uint32_t v, double sum, uint32_t, Tally &t) const {
+  const double d = 0.85;
+  double nv = __dadd_rn(1.0 - d, __dmul_rn(d, sum));
+  if (!last) {
+    uint32_t od = out_deg[v];
+    if (od > 0) {
+      nv = __ddiv_rn(nv, (double)od);
+      t.delta += __dmul_rn(fabs(__dadd_rn(nv, -curr[v])), (double)od);
+    } else {
+      t.delta += fabs(__dadd_rn(nv, -curr[v]));
+    }
+  }
+  next[v] = nv;
+  return false;
+}
+
+template <>
+__device__ __forceinline__ bool PrPull<float>::finish(uint32_t v, float sum, uint32_t, Tally &t) const {
+  const float d = 0.85f;
+  float nv = __fadd_rn(1.0f - d, __fmul_rn(d, sum));
+  if (!last) {
+    uint32_t od = out_deg[v];
+    if (od > 0) {
+      nv = __fdiv_rn(nv, (float)od);
+      t.delta += (double)fabsf(__fadd_rn(nv, -curr[v])) * (double)od;
+    } else {
+      t.delta += (double)fabsf(__fadd_rn(nv, -curr[v]));
+    }
+  }
+  next[v] = nv;
+  return false;
+}
+
+template <typename T>
+__global__ void pr_init(T *curr, const uint32_t *out_deg, uint32_t V) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x) {
+    uint32_t od = out_deg[v];
+    curr[v] = od > 0 ? T(1) / (T)od : T(1);
+  }
+}
+
+template <typename T>
+static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_host, gg_run_stats *st) {
+  if (iterations < 0) {
+    set_error("iterations must be >= 0");
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  const uint32_t V = g->V;
+  T *buf[2];
+  Counters *per_iter;
+  GG_TRY(ws(g, WS_S2, (size_t)V, &buf[0]));
+  GG_TRY(ws(g, WS_S3, (size_t)V, &buf[1]));
+  GG_TRY(ws(g, WS_HUBSUM, (size_t)(iterations > 0 ? iterations : 1), &per_iter));
+  Launch L(g);
+  Trace tr(st, g);
+  cudaStream_t s = g->stream;
+  GG_TRY(timed_begin(g));
+  GG_CUDA(cudaMemsetAsync(per_iter, 0, sizeof(Counters) * (iterations > 0 ? iterations : 1), s));
+  pr_init<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[0], g->out.deg, V);
+  L.launches += 1;
+  int cur = 0;
+  // active = all: active_edges = sum of out_degree = adjacency entries
+  unsigned long long ae = g->nadj;
+  for (int i = 0; i < iterations; i++) {
+    tr.add(ae < g->E / 20 ? 0 : 1, ae, V);
+    PrPull<T> op{buf[cur], buf[cur ^ 1], g->out.deg, i == iterations - 1};
+    GG_TRY(tr.kbegin());
+    pull_reduce<PrPull<T>><<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL, op, ActOut(),
+                                                                   per_iter + i);
+    GG_TRY(tr.kend());
+    L.launches += 1;
+    GG_CUDA(cudaGetLastError());
+    cur ^= 1;
+  }
+  GG_TRY(timed_end(g, st, L.launches));
+  GG_TRY(tr.collect());
+  if (deltas_host && iterations > 0) {
+    Counters *hc = new Counters[iterations];
+    cudaError_t e = cudaMemcpy(hc, per_iter, sizeof(Counters) * iterations, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) {
+      deltas_host[0] = 1.0;  // process_vertices returns 1 per vertex; divided by |V|
+      for (int i = 1; i < iterations; i++) deltas_host[i] = hc[i - 1].delta / V;
+    }
+    delete[] hc;
+    GG_CUDA(e);
+  }
+  if (ranks_host) GG_CUDA(cudaMemcpy(ranks_host, buf[cur], sizeof(T) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = buf[cur];
+  g->result[1] = nullptr;
+  return GG_OK;
+}
+
+// ------------------------------------------------------------------ process_vertices
+__global__ void active_edges_kernel(const uint32_t *__restrict__ bm, size_t words, const uint32_t *__restrict__ deg,
+                                    uint32_t V, Counters *ctr) {
+  Tally t;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t w = bm[i];
+    while (w) {
+      uint32_t b = __ffs(w) - 1;
+      w &= w - 1;
+      size_t v = i * 32 + b;
+      if (v < V) t.edges += deg[v];
+    }
+  }
+  t.flush(ctr);
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_bfs(gg_graph *g, uint32_t root, uint32_t *parent, gg_run_stats *stats) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return bfs_run(g, root, parent, stats);
+}
+
+int gg_pagerank(gg_graph *g, int iterations, double *ranks, double *deltas, gg_run_stats *stats) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return pr_run<double>(g, iterations, ranks, deltas, stats);
+}
+
+int gg_pagerank_f32(gg_graph *g, int iterations, float *ranks, double *deltas, gg_run_stats *stats) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return pr_run<float>(g, iterations, ranks, deltas, stats);
+}
+
+int gg_active_edges(gg_graph *g, const uint64_t *active_bitmap, uint64_t *active_edges) {
+  if (!g || !active_bitmap || !active_edges) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  size_t words = bitmap_words32(g->V);
+  uint32_t *bm;
+  GG_TRY(ws(g, WS_BM3, words, &bm));
+  GG_CUDA(cudaMemcpyAsync(bm, active_bitmap, words * 4, cudaMemcpyHostToDevice, g->stream));
+  GG_TRY(counters_reset(g));
+  active_edges_kernel<<<grid_for(words, 256, g->num_sms), 256, 0, g->stream>>>(bm, words, g->out.deg, g->V,
+                                                                              g->ws.ctr);
+  GG_CUDA(cudaGetLastError());
+  Counters c;
+  GG_TRY(counters_read(g, &c));
+  *active_edges = c.edges;
+  return GG_OK;
+}
+
+}  // extern "C"

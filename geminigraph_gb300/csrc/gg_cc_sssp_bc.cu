@@ -1,0 +1,503 @@
+// CC (toolkits/cc.cpp), SSSP (toolkits/sssp.cpp) and BC (toolkits/bc.cpp,
+// compute) on the device engine.
+#include <vector>
+
+#include "gg_engine.cuh"
+
+namespace gg {
+
+constexpr uint32_t PULL_SMALL_R = 32;
+
+// ------------------------------------------------------------------ CC
+// Sparse slot (cc.cpp:48-59): msg = label of the source at the start of the
+// call (snapshot); a lower msg lowers label[dst] and activates dst.
+struct CcPush {
+  uint32_t *label;
+  const uint32_t *msg;
+  __device__ __forceinline__ bool push(uint32_t, uint32_t i, uint32_t dst, float) const {
+    uint32_t m = msg[i];
+    if (m < *(volatile uint32_t *)(label + dst)) {
+      atomicMin(label + dst, m);
+      return true;
+    }
+    return false;
+  }
+};
+
+// Dense signal + slot (cc.cpp:60-79): msg = min(dst, labels of all
+// in-neighbours); read from cur, written to nxt.
+struct CcPull {
+  using Acc = uint32_t;
+  const uint32_t *cur;
+  uint32_t *nxt;
+  __device__ __forceinline__ bool want(uint32_t) const { return true; }
+  __device__ __forceinline__ uint32_t identity(uint32_t v) const { return v; }
+  __device__ __forceinline__ uint32_t identity_coop() const { return 0xffffffffu; }
+  __device__ __forceinline__ uint32_t gather(const Dir &d, unsigned long long k) const { return cur[d.nbr[k]]; }
+  __device__ __forceinline__ uint32_t combine(uint32_t a, uint32_t b) const { return b < a ? b : a; }
+  __device__ __forceinline__ uint32_t warp_combine(uint32_t x) const { return warp_min(x); }
+  __device__ __forceinline__ bool finish(uint32_t v, uint32_t m, uint32_t, Tally &) const {
+    uint32_t c = cur[v];
+    if (m < c) {
+      nxt[v] = m;
+      return true;
+    }
+    nxt[v] = c;
+    return false;
+  }
+};
+
+// ------------------------------------------------------------------ SSSP
+// Lowers *p to v if v is smaller; true if this call lowered it (write_min,
+// core/atomic.hpp:35-42).  Non-negative floats order like their int bits;
+// negative floats order like the reverse of their unsigned bits, and any
+// stored value of the other sign compares correctly in both forms.
+__device__ __forceinline__ bool atomic_min_float(float *p, float v) {
+  if (!(v < 0.0f)) {
+    int old = atomicMin((int *)p, __float_as_int(v));
+    return __int_as_float(old) > v;
+  }
+  unsigned old = atomicMax((unsigned *)p, __float_as_uint(v));
+  return __uint_as_float(old) > v;
+}
+
+struct SsspPush {
+  float *dist;
+  const float *msg;
+  __device__ __forceinline__ bool push(uint32_t, uint32_t i, uint32_t dst, float w) const {
+    float relax = __fadd_rn(msg[i], w);
+    if (relax < *(volatile float *)(dist + dst)) return atomic_min_float(dist + dst, relax);
+    return false;
+  }
+};
+
+// sssp.cpp:60-80: the dense signal takes the min over ALL in-edges (its
+// active check is commented out, sssp.cpp:64-70); INF = 1e9.
+struct SsspPull {
+  using Acc = float;
+  const float *cur;
+  float *nxt;
+  __device__ __forceinline__ bool want(uint32_t) const { return true; }
+  __device__ __forceinline__ float identity(uint32_t) const { return 1e9f; }
+  __device__ __forceinline__ float identity_coop() const { return 1e9f; }
+  __device__ __forceinline__ float gather(const Dir &d, unsigned long long k) const {
+    return __fadd_rn(cur[d.nbr[k]], d.w[k]);
+  }
+  __device__ __forceinline__ float combine(float a, float b) const { return b < a ? b : a; }
+  __device__ __forceinline__ float warp_combine(float x) const { return warp_min(x); }
+  __device__ __forceinline__ bool finish(uint32_t v, float m, uint32_t, Tally &) const {
+    float c = cur[v];
+    if (m < c) {
+      nxt[v] = m;
+      return true;
+    }
+    nxt[v] = c;
+    return false;
+  }
+};
+
+// Runs the CC / SSSP frontier loop: both toolkits loop while the slots
+// activate something, with a message snapshot for push calls and two state
+// buffers for pull calls.
+template <typename T, class PushOp, class PullOp>
+static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
+                      uint32_t n, unsigned long long ae, Trace &tr, Launch &L, T **result) {
+  const uint32_t V = g->V;
+  const size_t words = bitmap_words32(V);
+  cudaStream_t s = g->stream;
+  Counters *ctr = g->ws.ctr;
+  T *cur = state0, *nxt = state1;
+  uint32_t *q[2] = {q0, q1};
+  uint32_t *bm[2] = {bm0, bm1};
+  T *msg;
+  GG_TRY(ws(g, WS_MSG, (size_t)V + 1, &msg));
+  int c_i = 0;
+  while (n > 0) {
+    bool sparse = ae < g->E / 20;
+    tr.add(sparse ? 0 : 1, ae, 0);
+    int nx = c_i ^ 1;
+    GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
+    GG_TRY(counters_reset(g));
+    ActOut a;
+    a.active_out = bm[nx];
+    a.q_out = q[nx];
+    a.qlen = &ctr->qlen;
+    a.out_deg = g->out.deg;
+    if (sparse) {
+      if (ae > 0) {
+        gather_by_queue<T><<<grid_for(n, 256, g->num_sms), 256, 0, s>>>(q[c_i], n, cur, msg);
+        unsigned long long *P;
+        GG_TRY(L.scan_queue_degrees(q[c_i], n, g->out.deg, &P));
+        GG_TRY(tr.kbegin());
+        push_lb<PushOp><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[c_i], P, n, ae, g->out, PushOp{cur, msg}, a,
+                                                                   ctr);
+        GG_TRY(tr.kend());
+        L.launches += 2;
+      }
+    } else {
+      GG_TRY(tr.kbegin());
+      pull_reduce<PullOp><<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL_R, PullOp{cur, nxt}, a,
+                                                                  ctr);
+      GG_TRY(tr.kend());
+      L.launches += 1;
+      T *t = cur;
+      cur = nxt;
+      nxt = t;
+    }
+    GG_CUDA(cudaGetLastError());
+    Counters c;
+    GG_TRY(counters_read(g, &c));
+    n = c.qlen;
+    ae = c.edges;
+    tr.set_activated(c.activated);
+    c_i = nx;
+  }
+  *result = cur;
+  return GG_OK;
+}
+
+static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
+  GG_CUDA(cudaSetDevice(g->device));
+  const uint32_t V = g->V;
+  const size_t words = bitmap_words32(V);
+  uint32_t *lab[2], *bm[2], *q[2];
+  GG_TRY(ws(g, WS_S0, V, &lab[0]));
+  GG_TRY(ws(g, WS_S1, V, &lab[1]));
+  GG_TRY(ws(g, WS_BM1, words, &bm[0]));
+  GG_TRY(ws(g, WS_BM2, words, &bm[1]));
+  GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
+  GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
+  Launch L(g);
+  Trace tr(st, g);
+  cudaStream_t s = g->stream;
+  GG_TRY(timed_begin(g));
+  // label[v] = v over active_in = all (cc.cpp:31-37)
+  iota_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(lab[0], V);
+  iota_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(q[0], V);
+  bitmap_fill<<<grid_for(words, 256, g->num_sms), 256, 0, s>>>(bm[0], words, V);
+  L.launches += 3;
+  GG_CUDA(cudaGetLastError());
+  uint32_t *res = nullptr;
+  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, g->nadj, tr, L,
+                                               &res)));
+  GG_TRY(timed_end(g, st, L.launches));
+  GG_TRY(tr.collect());
+  if (label_host) GG_CUDA(cudaMemcpy(label_host, res, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = res;
+  g->result[1] = nullptr;
+  return GG_OK;
+}
+
+__global__ void sssp_root(float *dist, uint32_t root, uint32_t *active, uint32_t *q, const uint32_t *out_deg,
+                          Counters *ctr) {
+  dist[root] = 0.0f;
+  active[root >> 5] |= 1u << (root & 31);
+  q[0] = root;
+  ctr->edges = out_deg[root];
+}
+
+static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *st) {
+  if (!g->weighted) {
+    set_error("sssp needs a weighted graph");
+    return GG_ERR_UNWEIGHTED;
+  }
+  if (root >= g->V) {
+    set_error("root %u >= vertices %u", root, g->V);
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  const uint32_t V = g->V;
+  const size_t words = bitmap_words32(V);
+  float *dist[2];
+  uint32_t *bm[2], *q[2];
+  GG_TRY(ws(g, WS_S0, V, &dist[0]));
+  GG_TRY(ws(g, WS_S1, V, &dist[1]));
+  GG_TRY(ws(g, WS_BM1, words, &bm[0]));
+  GG_TRY(ws(g, WS_BM2, words, &bm[1]));
+  GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
+  GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
+  Launch L(g);
+  Trace tr(st, g);
+  cudaStream_t s = g->stream;
+  GG_TRY(timed_begin(g));
+  GG_CUDA(cudaMemsetAsync(bm[0], 0, words * 4, s));
+  GG_TRY(counters_reset(g));
+  fill_kernel<float><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(dist[0], V, 1e9f);
+  sssp_root<<<1, 1, 0, s>>>(dist[0], root, bm[0], q[0], g->out.deg, g->ws.ctr);
+  L.launches += 2;
+  GG_CUDA(cudaGetLastError());
+  Counters c;
+  GG_TRY(counters_read(g, &c));
+  float *res = nullptr;
+  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1, c.edges, tr, L,
+                                                &res)));
+  GG_TRY(timed_end(g, st, L.launches));
+  GG_TRY(tr.collect());
+  if (dist_host) GG_CUDA(cudaMemcpy(dist_host, res, sizeof(float) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = res;
+  g->result[1] = nullptr;
+  return GG_OK;
+}
+
+// ------------------------------------------------------------------ BC
+// Forward sparse slot (bc.cpp:58-69): unvisited dst gains the source's path
+// count; the first contribution (old value 0) activates dst.
+struct BcFwdPush {
+  double *np;
+  const uint32_t *visited;
+  __device__ __forceinline__ bool push(uint32_t src, uint32_t, uint32_t dst, float) const {
+    if (bm_test(visited, dst)) return false;
+    return atomicAdd(np + dst, np[src]) == 0.0;
+  }
+};
+
+// Forward dense (bc.cpp:70-89): an unvisited vertex sums the path counts of
+// its active in-neighbours.
+struct BcFwdPull {
+  using Acc = double;
+  double *np;
+  const uint32_t *active_in;
+  const uint32_t *visited;
+  __device__ __forceinline__ bool want(uint32_t v) const { return !bm_test(visited, v); }
+  __device__ __forceinline__ double identity(uint32_t) const { return 0.0; }
+  __device__ __forceinline__ double identity_coop() const { return 0.0; }
+  __device__ __forceinline__ double gather(const Dir &d, unsigned long long k) const {
+    uint32_t s = d.nbr[k];
+    return bm_test_ldg(active_in, s) ? np[s] : 0.0;
+  }
+  __device__ __forceinline__ double combine(double a, double b) const { return a + b; }
+  __device__ __forceinline__ double warp_combine(double x) const { return warp_sum(x); }
+  __device__ __forceinline__ bool finish(uint32_t v, double sum, uint32_t, Tally &) const {
+    if (sum > 0.0) {
+      np[v] += sum;
+      return true;
+    }
+    return false;
+  }
+};
+
+// Backward sparse slot (bc.cpp:130-138) on the transposed graph.
+struct BcBwdPush {
+  double *dep;
+  const uint32_t *visited;
+  __device__ __forceinline__ bool push(uint32_t src, uint32_t, uint32_t dst, float) const {
+    if (!bm_test(visited, dst)) atomicAdd(dep + dst, dep[src]);
+    return false;
+  }
+};
+
+// Backward dense (bc.cpp:139-155): unvisited vertices sum the dependencies
+// of their in-neighbours (on the transposed graph) in the current level.
+struct BcBwdPull {
+  using Acc = double;
+  double *dep;
+  const uint32_t *level;
+  const uint32_t *visited;
+  __device__ __forceinline__ bool want(uint32_t v) const { return !bm_test(visited, v); }
+  __device__ __forceinline__ double identity(uint32_t) const { return 0.0; }
+  __device__ __forceinline__ double identity_coop() const { return 0.0; }
+  __device__ __forceinline__ double gather(const Dir &d, unsigned long long k) const {
+    uint32_t s = d.nbr[k];
+    return bm_test_ldg(level, s) ? dep[s] : 0.0;
+  }
+  __device__ __forceinline__ double combine(double a, double b) const { return a + b; }
+  __device__ __forceinline__ double warp_combine(double x) const { return warp_sum(x); }
+  __device__ __forceinline__ bool finish(uint32_t v, double sum, uint32_t deg, Tally &) const {
+    if (deg > 0) dep[v] += sum;
+    return false;
+  }
+};
+
+__global__ void bc_root(double *np, uint32_t root, uint32_t *visited, uint32_t *active, uint32_t *qlev,
+                        const uint32_t *out_deg, const uint32_t *in_deg, Counters *ctr) {
+  np[root] = 1.0;
+  visited[root >> 5] |= 1u << (root & 31);
+  active[root >> 5] |= 1u << (root & 31);
+  qlev[0] = root;
+  ctr->edges = out_deg[root];
+  ctr->in_edges = in_deg[root];
+}
+
+// inv_num_paths = 1 / num_paths, dependencies = 0 (bc.cpp:103-111).
+__global__ void bc_invert(double *np, double *dep, uint32_t V) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x) {
+    np[v] = 1.0 / np[v];
+    dep[v] = 0.0;
+  }
+}
+
+// process_vertices over one level: visited |= level, dep += inv (bc.cpp:113-120,157-164).
+__global__ void bc_level_apply(const uint32_t *q, uint32_t n, uint32_t *visited, double *dep, const double *inv) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t v = q[i];
+    atomicOr(visited + (v >> 5), 1u << (v & 31));
+    dep[v] += inv[v];
+  }
+}
+
+// dependencies = (dep - inv) / inv (bc.cpp:170-176).
+__global__ void bc_final(double *dep, const double *inv, uint32_t V) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    dep[v] = (dep[v] - inv[v]) / inv[v];
+}
+
+static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host, gg_run_stats *st) {
+  if (root >= g->V) {
+    set_error("root %u >= vertices %u", root, g->V);
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  const uint32_t V = g->V;
+  const size_t words = bitmap_words32(V);
+  double *np, *dep;
+  uint32_t *visited, *bm[2], *lvbm, *qlev;
+  GG_TRY(ws(g, WS_S2, V, &np));
+  GG_TRY(ws(g, WS_S3, V, &dep));
+  GG_TRY(ws(g, WS_BM0, words, &visited));
+  GG_TRY(ws(g, WS_BM1, words, &bm[0]));
+  GG_TRY(ws(g, WS_BM2, words, &bm[1]));
+  GG_TRY(ws(g, WS_BM3, words, &lvbm));
+  GG_TRY(ws(g, WS_QLEV, (size_t)V + 2, &qlev));
+  Launch L(g);
+  Trace tr(st, g);
+  cudaStream_t s = g->stream;
+  Counters *ctr = g->ws.ctr;
+  GG_TRY(timed_begin(g));
+  GG_CUDA(cudaMemsetAsync(visited, 0, words * 4, s));
+  GG_CUDA(cudaMemsetAsync(bm[0], 0, words * 4, s));
+  GG_TRY(counters_reset(g));
+  fill_kernel<double><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(np, V, 0.0);
+  bc_root<<<1, 1, 0, s>>>(np, root, visited, bm[0], qlev, g->out.deg, g->in.deg, ctr);
+  L.launches += 2;
+  GG_CUDA(cudaGetLastError());
+  Counters c;
+  GG_TRY(counters_read(g, &c));
+  // level L occupies qlev[lev_off[L], lev_off[L+1]); lev_out/in = degree sums
+  std::vector<uint64_t> lev_off{0, 1}, lev_out{c.edges}, lev_in{c.in_edges};
+  int cur = 0;
+  uint32_t n = 1;
+  while (n > 0) {
+    size_t L_ = lev_off.size() - 2;
+    unsigned long long ae = lev_out[L_];
+    bool sparse = ae < g->E / 20;
+    tr.add(sparse ? 0 : 1, ae, 0);
+    int nx = cur ^ 1;
+    GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
+    GG_TRY(counters_reset(g));
+    ActOut a;
+    a.active_out = bm[nx];
+    a.q_out = qlev + lev_off.back();
+    a.qlen = &ctr->qlen;
+    a.out_deg = g->out.deg;
+    a.in_deg = g->in.deg;
+    const uint32_t *qin = qlev + lev_off[L_];
+    if (sparse) {
+      if (ae > 0) {
+        unsigned long long *P;
+        GG_TRY(L.scan_queue_degrees(qin, n, g->out.deg, &P));
+        GG_TRY(tr.kbegin());
+        push_lb<BcFwdPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(qin, P, n, ae, g->out, BcFwdPush{np, visited},
+                                                                      a, ctr);
+        GG_TRY(tr.kend());
+        L.launches += 1;
+      }
+    } else {
+      GG_TRY(tr.kbegin());
+      pull_reduce<BcFwdPull><<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL_R,
+                                                                     BcFwdPull{np, bm[cur], visited}, a, ctr);
+      GG_TRY(tr.kend());
+      L.launches += 1;
+    }
+    GG_CUDA(cudaGetLastError());
+    GG_TRY(counters_read(g, &c));
+    tr.set_activated(c.activated);
+    // visited |= active_out (bc.cpp:91-98)
+    bitmap_or<<<grid_for(words, 256, g->num_sms), 256, 0, s>>>(visited, bm[nx], words);
+    L.launches += 1;
+    n = c.qlen;
+    lev_off.push_back(lev_off.back() + n);
+    lev_out.push_back(c.edges);
+    lev_in.push_back(c.in_edges);
+    cur = nx;
+  }
+  // levels 0..top; level `top` is the empty set the last forward call produced
+  const int top = (int)lev_off.size() - 2;
+  bc_invert<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(np, dep, V);
+  GG_CUDA(cudaMemsetAsync(visited, 0, words * 4, s));
+  L.launches += 1;
+  // backward on the transposed graph: push over the CSC, pull over the CSR
+  const Dir &tout = g->in, &tin = g->out;
+  for (int lev = top; lev >= 1; lev--) {
+    uint32_t ln = (uint32_t)(lev_off[lev + 1] - lev_off[lev]);
+    const uint32_t *ql = qlev + lev_off[lev];
+    unsigned long long ae = lev_in[lev];
+    bool sparse = ae < g->E / 20;
+    tr.add(sparse ? 0 : 1, ae, 0);
+    if (sparse) {
+      if (ae > 0) {
+        unsigned long long *P;
+        GG_TRY(L.scan_queue_degrees(ql, ln, tout.deg, &P));
+        GG_TRY(tr.kbegin());
+        push_lb<BcBwdPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(ql, P, ln, ae, tout, BcBwdPush{dep, visited},
+                                                                      ActOut(), ctr);
+        GG_TRY(tr.kend());
+        L.launches += 1;
+      }
+    } else {
+      GG_CUDA(cudaMemsetAsync(lvbm, 0, words * 4, s));
+      if (ln) bitmap_from_queue<<<grid_for(ln, 256, g->num_sms), 256, 0, s>>>(ql, ln, lvbm);
+      GG_TRY(tr.kbegin());
+      pull_reduce<BcBwdPull><<<L.pull_grid(), PULL_THREADS, 0, s>>>(tin, V, PULL_SMALL_R,
+                                                                     BcBwdPull{dep, lvbm, visited}, ActOut(), ctr);
+      GG_TRY(tr.kend());
+      L.launches += 2;
+    }
+    uint32_t pn = (uint32_t)(lev_off[lev] - lev_off[lev - 1]);
+    if (pn)
+      bc_level_apply<<<grid_for(pn, 256, g->num_sms), 256, 0, s>>>(qlev + lev_off[lev - 1], pn, visited, dep, np);
+    L.launches += 1;
+    GG_CUDA(cudaGetLastError());
+  }
+  bc_final<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(dep, np, V);
+  L.launches += 1;
+  GG_CUDA(cudaGetLastError());
+  GG_TRY(timed_end(g, st, L.launches));
+  GG_TRY(tr.collect());
+  if (dep_host) GG_CUDA(cudaMemcpy(dep_host, dep, sizeof(double) * V, cudaMemcpyDeviceToHost));
+  if (inv_host) GG_CUDA(cudaMemcpy(inv_host, np, sizeof(double) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = dep;
+  g->result[1] = np;
+  return GG_OK;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_cc(gg_graph *g, uint32_t *label, gg_run_stats *stats) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return cc_run(g, label, stats);
+}
+
+int gg_sssp(gg_graph *g, uint32_t root, float *distance, gg_run_stats *stats) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return sssp_run(g, root, distance, stats);
+}
+
+int gg_bc(gg_graph *g, uint32_t root, double *dependencies, double *inv_num_paths, gg_run_stats *stats) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return bc_run(g, root, dependencies, inv_num_paths, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,261 @@
+// Shared device-side definitions of the GB300 edge-processing engine.
+//
+// Memory layout in HBM (one graph, one GPU):
+//   out.off  uint64[V+1]  CSR offsets (grouped by source, "outgoing")
+//   out.nbr  uint32[A]    CSR neighbour ids, sorted ascending in each list
+//   out.w    float[A]     CSR edge weights (weighted graphs only), parallel array
+//   out.deg  uint32[V]    out_degree (core/graph.hpp:110)
+//   in.*                  the same for the CSC (grouped by destination)
+// A = adjacency entries per direction = E (directed) or 2E (symmetric, where
+// in.* aliases out.*, as core/graph.hpp:733-738 does).
+// Vertex subsets are bitmaps in the reference's layout (core/bitmap.hpp:
+// bit v%64 of 64-bit word v/64, V/64+1 words).  On a little-endian device the
+// same bytes read as uint32 words give bit v%32 of word v/32, so kernels use
+// 32-bit words and one warp owns the word of its 32 consecutive vertices.
+#ifndef GG_COMMON_CUH
+#define GG_COMMON_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gemini_gb300.h"
+
+#define GG_WARP 32
+#define GG_FULL 0xffffffffu
+
+namespace gg {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t e, const char *what);
+
+#define GG_CUDA(call)                                 \
+  do {                                                \
+    cudaError_t _e = (call);                          \
+    if (_e != cudaSuccess) return ::gg::cuda_status(_e, #call); \
+  } while (0)
+
+#define GG_TRY(call)            \
+  do {                          \
+    int _s = (call);            \
+    if (_s != GG_OK) return _s; \
+  } while (0)
+
+// ---------------------------------------------------------------- graph
+struct Dir {
+  uint64_t *off = nullptr;
+  uint32_t *nbr = nullptr;
+  float *w = nullptr;
+  uint32_t *deg = nullptr;
+  uint32_t *hubs = nullptr;   // vertices with deg > hub_threshold, ascending
+  uint32_t nhubs = 0;
+};
+
+// Per-call counters written by the activation epilogue of every edge kernel.
+struct Counters {
+  unsigned long long edges;     // sum of out_degree over newly activated vertices
+  unsigned long long in_edges;  // sum of in_degree over newly activated vertices
+  unsigned int activated;       // vertices whose active_out bit this call set
+  unsigned int qlen;            // entries appended to the output queue
+  double delta;                 // PageRank delta accumulator
+  unsigned int err;             // device-side error flag (bounds checks)
+  unsigned int pad;
+};
+
+enum WsSlot {
+  WS_BM0, WS_BM1, WS_BM2, WS_BM3,       // bitmaps
+  WS_Q0, WS_Q1, WS_QLEV,                // queues / level order
+  WS_PREFIX,                            // uint64 prefix of queue degrees
+  WS_MSG,                               // per-queue-entry message snapshot (4 or 8 B)
+  WS_S0, WS_S1, WS_S2, WS_S3,           // vertex state arrays
+  WS_SCAN,                              // scan scratch
+  WS_HUBSUM,                            // per-hub partial results
+  WS_NSLOTS
+};
+
+struct Workspace {
+  void *ptr[WS_NSLOTS] = {};
+  size_t bytes[WS_NSLOTS] = {};
+  Counters *ctr = nullptr;       // device
+  Counters *ctr_host = nullptr;  // pinned mirror
+};
+
+}  // namespace gg
+
+struct gg_graph {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint32_t V = 0;
+  uint64_t E = 0;
+  uint64_t nadj = 0;
+  int weighted = 0, symmetric = 0, transposed = 0;
+  gg::Dir out, in;
+  gg::Workspace ws;
+  uint64_t graph_bytes = 0;
+  int num_sms = 0;
+  uint32_t hub_threshold = 0;
+  const void *result[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> evpool;  // events for per-call kernel timing
+};
+
+namespace gg {
+
+// ---------------------------------------------------------------- host helpers
+int ws_get(gg_graph *g, WsSlot slot, size_t bytes, void **out);
+template <typename T>
+inline int ws(gg_graph *g, WsSlot slot, size_t count, T **out) {
+  return ws_get(g, slot, count * sizeof(T), (void **)out);
+}
+int ws_free_all(gg_graph *g);
+int counters_reset(gg_graph *g);
+int counters_read(gg_graph *g, Counters *out);
+
+inline size_t bitmap_words32(uint32_t V) { return 2 * ((size_t)V / 64 + 1); }
+inline unsigned grid_for(size_t work, int threads, int num_sms, int per_sm = 8) {
+  size_t blocks = (work + threads - 1) / threads;
+  size_t cap = (size_t)num_sms * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (unsigned)blocks;
+}
+
+// Exclusive scan of `in(i)` for i < n into out[0..n] (out[n] = total).
+// Three-phase (tile reduce, recursive scan of tile sums, tile scan): no
+// inter-block waiting.  scratch must hold scan_scratch_elems(n) elements.
+size_t scan_scratch_elems(size_t n);
+
+// Stats/trace helper for toolkits: one row per process_edges call, and, when
+// the caller passed call_ms, CUDA events around each call's edge kernel.
+struct Trace {
+  gg_run_stats *st;
+  gg_graph *g;
+  std::vector<int> ev_call;
+  std::vector<cudaEvent_t> ev;
+  Trace(gg_run_stats *s, gg_graph *gr) : st(s), g(gr) {
+    if (st) {
+      st->calls = 0;
+      st->active_edges_total = 0;
+      st->device_ms = 0;
+      st->kernel_launches = 0;
+    }
+  }
+  void add(int mode, uint64_t active_edges, uint64_t activated) {
+    if (!st) return;
+    int i = st->calls;
+    if (i < st->trace_capacity) {
+      if (st->mode) st->mode[i] = mode;
+      if (st->active_edges) st->active_edges[i] = active_edges;
+      if (st->activated) st->activated[i] = activated;
+      if (st->call_ms) st->call_ms[i] = 0.0;
+    }
+    st->calls = i + 1;
+    st->active_edges_total += active_edges;
+  }
+  void set_activated(uint64_t activated) {
+    if (!st) return;
+    int i = st->calls - 1;
+    if (i >= 0 && i < st->trace_capacity && st->activated) st->activated[i] = activated;
+  }
+  bool timing() const { return st && st->call_ms && st->calls >= 1 && st->calls - 1 < st->trace_capacity; }
+  int kbegin();
+  int kend();
+  int collect();  // after the stream has been synchronised
+};
+
+int timed_begin(gg_graph *g);
+int timed_end(gg_graph *g, gg_run_stats *st, int launches);
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ bool bm_test(const uint32_t *bm, uint32_t v) {
+  return (bm[v >> 5] >> (v & 31)) & 1u;
+}
+__device__ __forceinline__ bool bm_test_ldg(const uint32_t *__restrict__ bm, uint32_t v) {
+  return (__ldg(bm + (v >> 5)) >> (v & 31)) & 1u;
+}
+// Sets bit v; returns true if it was clear before (this thread activated v).
+__device__ __forceinline__ bool bm_set_atomic(uint32_t *bm, uint32_t v) {
+  uint32_t bit = 1u << (v & 31);
+  if (bm[v >> 5] & bit) return false;
+  return !(atomicOr(bm + (v >> 5), bit) & bit);
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(GG_FULL, x, o);
+  return x;
+}
+template <typename T>
+__device__ __forceinline__ T warp_min(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T y = __shfl_xor_sync(GG_FULL, x, o);
+    x = y < x ? y : x;
+  }
+  return x;
+}
+
+// Warp-aggregated append: every lane of the warp must call it.
+__device__ __forceinline__ void queue_push(bool pred, uint32_t v, uint32_t *q, unsigned *qlen) {
+  unsigned m = __ballot_sync(GG_FULL, pred);
+  if (!m) return;
+  unsigned lane = lane_id();
+  unsigned leader = __ffs(m) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(qlen, (unsigned)__popc(m));
+  base = __shfl_sync(GG_FULL, base, leader);
+  if (pred) q[base + __popc(m & lanemask_lt())] = v;
+}
+
+// Per-thread activation totals, flushed once per block.
+struct Tally {
+  unsigned long long edges = 0, in_edges = 0;
+  unsigned int activated = 0;
+  double delta = 0.0;
+  // all threads of the block must call flush
+  __device__ __forceinline__ void flush(Counters *ctr) {
+    __shared__ unsigned long long s_e[32], s_i[32];
+    __shared__ unsigned int s_a[32];
+    __shared__ double s_d[32];
+    unsigned long long e = warp_sum(edges), ie = warp_sum(in_edges);
+    unsigned int a = warp_sum(activated);
+    double dl = warp_sum(delta);
+    unsigned w = threadIdx.x >> 5, lane = lane_id();
+    if (lane == 0) {
+      s_e[w] = e;
+      s_i[w] = ie;
+      s_a[w] = a;
+      s_d[w] = dl;
+    }
+    __syncthreads();
+    if (w == 0) {
+      unsigned nw = (blockDim.x + 31) >> 5;
+      e = lane < nw ? s_e[lane] : 0ull;
+      ie = lane < nw ? s_i[lane] : 0ull;
+      a = lane < nw ? s_a[lane] : 0u;
+      dl = lane < nw ? s_d[lane] : 0.0;
+      e = warp_sum(e);
+      ie = warp_sum(ie);
+      a = warp_sum(a);
+      dl = warp_sum(dl);
+      if (lane == 0) {
+        if (e) atomicAdd(&ctr->edges, e);
+        if (ie) atomicAdd(&ctr->in_edges, ie);
+        if (a) atomicAdd(&ctr->activated, a);
+        if (dl != 0.0) atomicAdd(&ctr->delta, dl);
+      }
+    }
+  }
+};
+
+}  // namespace gg
+
+#endif

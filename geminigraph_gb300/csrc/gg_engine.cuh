@@ -1,0 +1,309 @@
+// Edge-processing engine: the GB300 form of Graph::process_edges
+// (core/graph.hpp:1492-1867) and Graph::process_vertices (:1406-1469).
+//
+// Reference semantics kept exactly:
+//  * switch: sparse iff active_edges < edges / 20 (:1509), active_edges =
+//    sum of out_degree over the active set (:1503-1508);
+//  * every signal of a call is computed before any slot of the call applies
+//    (messages are buffered, :1541-1556 and :1755-1793).  Push kernels read
+//    their message from a snapshot taken before the kernel (or from state no
+//    slot of the call can write); pull kernels that read a state array the
+//    same call writes use two buffers (read one, write the other).
+// Fused on the device:
+//  * signal + slot: the push kernel computes the slot for each edge of each
+//    queued vertex; the pull kernel gathers the in-list (signal) and applies
+//    the slot to its own vertex with a plain store (one writer per vertex);
+//  * the activation epilogue of every edge kernel sets the active_out bit,
+//    appends the vertex to the next queue and adds its out_degree to the
+//    next call's active_edges, so the switch of the next call and the
+//    process_vertices(active_out) count need no extra pass.
+#ifndef GG_ENGINE_CUH
+#define GG_ENGINE_CUH
+
+#include "gg_common.cuh"
+#include "gg_scan.cuh"
+
+namespace gg {
+
+constexpr uint32_t NONE32 = 0xffffffffu;
+constexpr int PUSH_THREADS = 256;
+constexpr int PUSH_TILE = PUSH_THREADS * 8;
+constexpr int PULL_THREADS = 256;
+
+// Where an edge kernel records activations.
+struct ActOut {
+  uint32_t *active_out = nullptr;  // bitmap; null: the call activates nothing
+  uint32_t *visited = nullptr;     // also set here when non-null
+  uint32_t *q_out = nullptr;       // next queue
+  unsigned *qlen = nullptr;
+  const uint32_t *out_deg = nullptr;
+  const uint32_t *in_deg = nullptr;  // optional: also sum in_degree
+};
+
+// Push activation: pred may be true for several lanes naming the same
+// vertex; the bitmap decides who appends.  All lanes must call.
+__device__ __forceinline__ void push_activate(bool pred, uint32_t v, const ActOut &a, Tally &t) {
+  bool fresh = false;
+  if (pred) {
+    fresh = bm_set_atomic(a.active_out, v);
+    if (fresh && a.visited) atomicOr(a.visited + (v >> 5), 1u << (v & 31));
+  }
+  queue_push(fresh, v, a.q_out, a.qlen);
+  if (fresh) {
+    t.activated += 1;
+    t.edges += a.out_deg[v];
+    if (a.in_deg) t.in_edges += a.in_deg[v];
+  }
+}
+
+// Pull activation: the warp owns bitmap word g (vertices 32g..32g+31), so the
+// word is written with plain stores.  All lanes must call.
+__device__ __forceinline__ void pull_activate(bool act, uint32_t v, size_t g, const ActOut &a, Tally &t) {
+  unsigned bits = __ballot_sync(GG_FULL, act);
+  if (lane_id() == 0 && bits) {
+    a.active_out[g] = bits;
+    if (a.visited) a.visited[g] |= bits;
+  }
+  queue_push(act, v, a.q_out, a.qlen);
+  if (act) {
+    t.activated += 1;
+    t.edges += a.out_deg[v];
+    if (a.in_deg) t.in_edges += a.in_deg[v];
+  }
+}
+
+__device__ __forceinline__ uint32_t upper_bound_u64(const unsigned long long *P, uint32_t lo, uint32_t hi,
+                                                    unsigned long long x) {
+  // first index in [lo, hi) with P[i] > x (hi if none)
+  while (lo < hi) {
+    uint32_t mid = lo + ((hi - lo) >> 1);
+    if (P[mid] <= x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------- push
+// Sparse mode (core/graph.hpp:1510-1663): for every queued vertex q[i] and
+// every out-edge, op.push(src, i, dst, w) applies the slot and returns
+// whether it may activate dst.  Work is split by EDGES: P is the exclusive
+// prefix of the queued vertices' degrees (P[n] = total), each tile of
+// PUSH_TILE consecutive edges is one block iteration, and each thread finds
+// its edge's vertex by binary search, so a hub's list is spread over as many
+// blocks as it needs and neighbour loads are coalesced.
+template <class Op>
+__global__ void __launch_bounds__(PUSH_THREADS)
+    push_lb(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
+            unsigned long long total, Dir d, Op op, ActOut act, Counters *ctr) {
+  __shared__ uint32_t s_lo, s_hi;
+  Tally t;
+  unsigned long long ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
+  for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    unsigned long long e0 = tile * PUSH_TILE;
+    unsigned long long e1 = e0 + PUSH_TILE < total ? e0 + PUSH_TILE : total;
+    if (threadIdx.x == 0) {
+      s_lo = upper_bound_u64(P, 0, n + 1, e0) - 1;
+      s_hi = upper_bound_u64(P, s_lo, n + 1, e1 - 1);  // one past the entry holding e1-1
+    }
+    __syncthreads();
+    uint32_t lo = s_lo, hi = s_hi;
+    __syncthreads();
+    for (unsigned long long base = e0; base < e1; base += PUSH_THREADS) {
+      unsigned long long e = base + threadIdx.x;
+      bool valid = e < e1;
+      bool pred = false;
+      uint32_t dst = 0;
+      if (valid) {
+        uint32_t i = upper_bound_u64(P, lo, hi, e) - 1;
+        uint32_t src = q[i];
+        unsigned long long k = d.off[src] + (e - P[i]);
+        dst = d.nbr[k];
+        float w = d.w ? d.w[k] : 0.0f;
+        pred = op.push(src, i, dst, w);
+      }
+      if (act.active_out) push_activate(pred, dst, act, t);
+    }
+  }
+  t.flush(ctr);
+}
+
+// ---------------------------------------------------------------- pull
+// Dense mode (core/graph.hpp:1664-1855), reduction form.  One warp owns 32
+// consecutive vertices.  For each vertex with op.want(v): acc = identity,
+// combined over the in-list with op.gather / op.combine -- serially by its
+// own lane when in-degree <= small, else by the whole warp (strided loads,
+// shuffle reduction); then op.finish(v, acc, deg) applies the slot and
+// returns whether v is activated.  Op::Acc is the message type.
+template <class Op>
+__global__ void __launch_bounds__(PULL_THREADS)
+    pull_reduce(Dir d, uint32_t V, uint32_t small, Op op, ActOut act, Counters *ctr) {
+  using Acc = typename Op::Acc;
+  Tally t;
+  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  size_t groups = ((size_t)V + 31) / 32;
+  unsigned lane = lane_id();
+  for (size_t g = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); g < groups; g += nwarps) {
+    uint32_t v = (uint32_t)(g * 32 + lane);
+    bool todo = v < V && op.want(v);
+    unsigned long long b = 0, e = 0;
+    if (todo) {
+      b = d.off[v];
+      e = d.off[v + 1];
+    }
+    uint32_t deg = (uint32_t)(e - b);
+    Acc acc = op.identity(v);
+    if (todo && deg <= small) {
+      for (unsigned long long k = b; k < e; k++) acc = op.combine(acc, op.gather(d, k));
+    }
+    unsigned coop = __ballot_sync(GG_FULL, todo && deg > small);
+    while (coop) {
+      unsigned leader = __ffs(coop) - 1;
+      coop &= coop - 1;
+      unsigned long long lb = __shfl_sync(GG_FULL, b, leader), le = __shfl_sync(GG_FULL, e, leader);
+      Acc part = op.identity_coop();
+      for (unsigned long long k = lb + lane; k < le; k += 32) part = op.combine(part, op.gather(d, k));
+      part = op.warp_combine(part);
+      if (lane == leader) acc = op.combine(acc, part);
+    }
+    bool a = todo && op.finish(v, acc, deg, t);
+    if (act.active_out) pull_activate(a, v, g, act, t);
+  }
+  t.flush(ctr);
+}
+
+// BFS pull (toolkits/bfs.cpp:60-76): an unvisited vertex takes the FIRST
+// in-neighbour (in CSC order) that is in the active set as its parent.  The
+// cooperative scan keeps that order: the first 32-wide chunk with a hit wins
+// and inside it the lowest lane.
+static __global__ void __launch_bounds__(PULL_THREADS)
+    bfs_pull(Dir d, uint32_t V, uint32_t small, const uint32_t *__restrict__ active_in, uint32_t *parent,
+             ActOut act, Counters *ctr) {
+  Tally t;
+  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  size_t groups = ((size_t)V + 31) / 32;
+  unsigned lane = lane_id();
+  for (size_t g = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); g < groups; g += nwarps) {
+    uint32_t v = (uint32_t)(g * 32 + lane);
+    uint32_t vis = act.visited[g];
+    bool todo = v < V && !((vis >> lane) & 1u);
+    unsigned long long b = 0, e = 0;
+    if (todo) {
+      b = d.off[v];
+      e = d.off[v + 1];
+    }
+    uint32_t deg = (uint32_t)(e - b);
+    uint32_t found = NONE32;
+    if (todo && deg <= small) {
+      for (unsigned long long k = b; k < e; k++) {
+        uint32_t s = d.nbr[k];
+        if (bm_test_ldg(active_in, s)) {
+          found = s;
+          break;
+        }
+      }
+    }
+    unsigned coop = __ballot_sync(GG_FULL, todo && deg > small);
+    while (coop) {
+      unsigned leader = __ffs(coop) - 1;
+      coop &= coop - 1;
+      unsigned long long lb = __shfl_sync(GG_FULL, b, leader), le = __shfl_sync(GG_FULL, e, leader);
+      uint32_t fsrc = NONE32;
+      for (unsigned long long base = lb; base < le; base += 32) {
+        unsigned long long k = base + lane;
+        uint32_t s = 0;
+        bool hit = false;
+        if (k < le) {
+          s = d.nbr[k];
+          hit = bm_test_ldg(active_in, s);
+        }
+        unsigned m = __ballot_sync(GG_FULL, hit);
+        if (m) {
+          fsrc = __shfl_sync(GG_FULL, s, __ffs(m) - 1);
+          break;
+        }
+      }
+      if (lane == leader) found = fsrc;
+    }
+    bool a = found != NONE32;
+    if (a) parent[v] = found;
+    pull_activate(a, v, g, act, t);
+  }
+  t.flush(ctr);
+}
+
+// ---------------------------------------------------------------- small kernels
+// out[i] = src[q[i]]: the message snapshot of a push call's queued vertices.
+template <typename T>
+static __global__ void gather_by_queue(const uint32_t *__restrict__ q, uint32_t n, const T *__restrict__ src,
+                                       T *__restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = src[q[i]];
+}
+
+template <typename T>
+static __global__ void fill_kernel(T *__restrict__ a, size_t n, T v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+static __global__ void iota_u32(uint32_t *__restrict__ a, uint32_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    a[i] = (uint32_t)i;
+}
+
+// dst |= src, word by word.
+static __global__ void bitmap_or(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src, size_t words) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] |= src[i];
+}
+
+// Sets the bits of the n queued vertices.
+static __global__ void bitmap_from_queue(const uint32_t *__restrict__ q, uint32_t n, uint32_t *__restrict__ bm) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t v = q[i];
+    atomicOr(bm + (v >> 5), 1u << (v & 31));
+  }
+}
+
+// Bitmap::fill (core/bitmap.hpp:42-52): bits [0, V) set, the rest clear.
+static __global__ void bitmap_fill(uint32_t *__restrict__ bm, size_t words, uint32_t V) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x) {
+    size_t lo = i * 32;
+    uint32_t w;
+    if (lo + 32 <= V)
+      w = 0xffffffffu;
+    else if (lo >= V)
+      w = 0u;
+    else
+      w = (1u << (V - lo)) - 1u;
+    bm[i] = w;
+  }
+}
+
+// Launch helpers shared by the toolkits.
+struct Launch {
+  gg_graph *g;
+  int launches = 0;
+  explicit Launch(gg_graph *gr) : g(gr) {}
+  unsigned pull_grid() const { return grid_for(((size_t)g->V + 31) / 32 * 32, PULL_THREADS, g->num_sms, 8); }
+  unsigned push_grid(unsigned long long total) const {
+    unsigned long long tiles = (total + PUSH_TILE - 1) / PUSH_TILE;
+    unsigned long long cap = (unsigned long long)g->num_sms * 8;
+    return (unsigned)(tiles < 1 ? 1 : (tiles > cap ? cap : tiles));
+  }
+  int scan_queue_degrees(const uint32_t *q, uint32_t n, const uint32_t *deg, unsigned long long **P) {
+    unsigned long long *p = nullptr, *scratch = nullptr;
+    GG_TRY(ws(g, WS_PREFIX, (size_t)g->V + 2, &p));
+    GG_TRY(ws(g, WS_SCAN, scan_scratch_elems((size_t)g->V + 1), &scratch));
+    GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q, deg}, n, p, scratch, g->stream,
+                                                               &launches)));
+    *P = p;
+    return GG_OK;
+  }
+};
+
+}  // namespace gg
+
+#endif

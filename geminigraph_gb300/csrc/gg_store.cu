@@ -1,0 +1,800 @@
+// Graph store: edge list -> CSR (out) + CSC (in) on the device.
+//
+// Replaces Graph::load_directed (core/graph.hpp:771-1339) and
+// Graph::load_undirected_from_directed (core/graph.hpp:349-757).  The
+// reference makes five passes over the file with MPI self-shuffles and racing
+// fetch_add fills; here every direction is one stable LSD radix sort of
+// packed 64-bit (major << b | minor) keys on the device (b = bits of V-1),
+// followed by a boundary pass that writes the offsets.  Lists come out sorted
+// by neighbour id with duplicate edges in record order, so the build is
+// deterministic.  Degrees are offset differences; symmetric graphs sort the
+// records plus their reverses once and alias CSC = CSR (core/graph.hpp:733-738);
+// their degree therefore counts both endpoints (core/graph.hpp:393-399).
+#include <errno.h>
+#include <fcntl.h>
+#include <stdarg.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <thread>
+#include <vector>
+
+#include "gg_common.cuh"
+#include "gg_gen.h"
+#include "gg_scan.cuh"
+
+namespace gg {
+
+// ------------------------------------------------------------------ errors
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char *what) {
+  set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+  if (e == cudaErrorMemoryAllocation) return GG_ERR_NOMEM;
+  return GG_ERR_CUDA;
+}
+
+size_t scan_scratch_elems(size_t n) { return scan_scratch_elems_impl(n) + 1; }
+
+// ------------------------------------------------------------------ workspace
+int ws_get(gg_graph *g, WsSlot slot, size_t bytes, void **out) {
+  Workspace &w = g->ws;
+  if (bytes == 0) bytes = 16;
+  if (w.bytes[slot] < bytes) {
+    if (w.ptr[slot]) GG_CUDA(cudaFree(w.ptr[slot]));
+    w.ptr[slot] = nullptr;
+    w.bytes[slot] = 0;
+    GG_CUDA(cudaMalloc(&w.ptr[slot], bytes));
+    w.bytes[slot] = bytes;
+  }
+  *out = w.ptr[slot];
+  return GG_OK;
+}
+
+int ws_free_all(gg_graph *g) {
+  Workspace &w = g->ws;
+  for (int i = 0; i < WS_NSLOTS; i++) {
+    if (w.ptr[i]) cudaFree(w.ptr[i]);
+    w.ptr[i] = nullptr;
+    w.bytes[i] = 0;
+  }
+  if (w.ctr) cudaFree(w.ctr);
+  if (w.ctr_host) cudaFreeHost(w.ctr_host);
+  w.ctr = nullptr;
+  w.ctr_host = nullptr;
+  return GG_OK;
+}
+
+int counters_reset(gg_graph *g) {
+  GG_CUDA(cudaMemsetAsync(g->ws.ctr, 0, sizeof(Counters), g->stream));
+  return GG_OK;
+}
+
+int counters_read(gg_graph *g, Counters *out) {
+  GG_CUDA(cudaMemcpyAsync(g->ws.ctr_host, g->ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  *out = *g->ws.ctr_host;
+  return GG_OK;
+}
+
+int Trace::kbegin() {
+  if (!timing()) return GG_OK;
+  size_t need = ev.size() + 2;
+  while (g->evpool.size() < need) {
+    cudaEvent_t e;
+    GG_CUDA(cudaEventCreate(&e));
+    g->evpool.push_back(e);
+  }
+  cudaEvent_t e0 = g->evpool[ev.size()];
+  ev.push_back(e0);
+  ev_call.push_back(st->calls - 1);
+  GG_CUDA(cudaEventRecord(e0, g->stream));
+  return GG_OK;
+}
+
+int Trace::kend() {
+  if (!timing() || ev.size() % 2 == 0) return GG_OK;
+  cudaEvent_t e1 = g->evpool[ev.size()];
+  ev.push_back(e1);
+  GG_CUDA(cudaEventRecord(e1, g->stream));
+  return GG_OK;
+}
+
+int Trace::collect() {
+  if (!st || !st->call_ms) return GG_OK;
+  for (size_t i = 0; i + 1 < ev.size(); i += 2) {
+    float ms = 0;
+    GG_CUDA(cudaEventSynchronize(ev[i + 1]));
+    GG_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+    st->call_ms[ev_call[i / 2]] += ms;
+  }
+  ev.clear();
+  ev_call.clear();
+  return GG_OK;
+}
+
+int timed_begin(gg_graph *g) {
+  GG_CUDA(cudaEventRecord(g->ev0, g->stream));
+  return GG_OK;
+}
+
+int timed_end(gg_graph *g, gg_run_stats *st, int launches) {
+  GG_CUDA(cudaEventRecord(g->ev1, g->stream));
+  GG_CUDA(cudaEventSynchronize(g->ev1));
+  float ms = 0;
+  GG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+  if (st) {
+    st->device_ms = ms;
+    st->kernel_launches = launches;
+  }
+  return GG_OK;
+}
+
+// ------------------------------------------------------------------ radix sort
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 4096 keys per tile
+constexpr int RS_WARP_KEYS = 32 * RS_ITEMS;      // 512 consecutive keys per warp
+
+__global__ void __launch_bounds__(RS_THREADS) rs_upsweep(const uint64_t *__restrict__ keys, size_t n, int shift,
+                                                         uint32_t *__restrict__ counts, uint32_t ntiles) {
+  __shared__ uint32_t hist[256];
+  hist[threadIdx.x] = 0;
+  __syncthreads();
+  size_t base = (size_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+  for (int k = 0; k < RS_ITEMS; k++) {
+    size_t idx = base + (size_t)k * RS_THREADS + threadIdx.x;
+    if (idx < n) atomicAdd(&hist[(keys[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  counts[(size_t)threadIdx.x * ntiles + blockIdx.x] = hist[threadIdx.x];
+}
+
+// Stable scatter of one tile.  Warp w ranks keys [w*512, w*512+512) of the
+// tile in order (round r, lane) with __match_any_sync peer groups and a
+// warp-private digit histogram; warps are then offset by the per-digit prefix
+// over lower warps, and tiles by the digit-major scan of the upsweep counts.
+__global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint64_t *__restrict__ kin,
+                                                         const uint32_t *__restrict__ vin,
+                                                         uint64_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                                                         size_t n, int shift, const uint32_t *__restrict__ scanned,
+                                                         uint32_t ntiles) {
+  __shared__ uint32_t whist[RS_THREADS / 32][256];
+  __shared__ uint32_t gbase[256];
+  for (int i = threadIdx.x; i < (RS_THREADS / 32) * 256; i += RS_THREADS) (&whist[0][0])[i] = 0;
+  gbase[threadIdx.x] = scanned[(size_t)threadIdx.x * ntiles + blockIdx.x];
+  __syncthreads();
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const size_t base = (size_t)blockIdx.x * RS_TILE + (size_t)w * RS_WARP_KEYS;
+  uint64_t key[RS_ITEMS];
+  uint32_t val[RS_ITEMS];
+  uint32_t rank[RS_ITEMS];
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    size_t idx = base + (size_t)r * 32 + lane;
+    bool valid = idx < n;
+    key[r] = valid ? kin[idx] : 0ull;
+    val[r] = (vin && valid) ? vin[idx] : 0u;
+    uint32_t d = valid ? (uint32_t)((key[r] >> shift) & 255u) : 256u + lane;
+    unsigned peers = __match_any_sync(GG_FULL, d);
+    unsigned leader = __ffs(peers) - 1;
+    uint32_t cnt = valid ? whist[w][d] : 0u;
+    __syncwarp();
+    if (valid && lane == leader) whist[w][d] = cnt + __popc(peers);
+    __syncwarp();
+    rank[r] = cnt + __popc(peers & lanemask_lt());
+  }
+  __syncthreads();
+  {
+    uint32_t run = 0;
+#pragma unroll
+    for (int ww = 0; ww < RS_THREADS / 32; ww++) {
+      uint32_t t = whist[ww][threadIdx.x];
+      whist[ww][threadIdx.x] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; r++) {
+    size_t idx = base + (size_t)r * 32 + lane;
+    if (idx < n) {
+      uint32_t d = (uint32_t)((key[r] >> shift) & 255u);
+      uint32_t pos = gbase[d] + whist[w][d] + rank[r];
+      kout[pos] = key[r];
+      if (vout) vout[pos] = val[r];
+    }
+  }
+}
+
+// Sorts n keys (and optional values) on the low `key_bits` bits.  Returns the
+// buffers holding the result through *kres / *vres (either the inputs or the
+// alternates).
+static int radix_sort(gg_graph *g, uint64_t *k0, uint32_t *v0, uint64_t *k1, uint32_t *v1, size_t n, int key_bits,
+                      uint64_t **kres, uint32_t **vres) {
+  *kres = k0;
+  *vres = v0;
+  if (n <= 1) return GG_OK;
+  size_t ntiles = (n + RS_TILE - 1) / RS_TILE;
+  size_t ncounts = 256 * ntiles;
+  uint32_t *counts = nullptr, *scanned = nullptr, *scratch = nullptr;
+  GG_CUDA(cudaMalloc(&counts, sizeof(uint32_t) * ncounts));
+  GG_CUDA(cudaMalloc(&scanned, sizeof(uint32_t) * (ncounts + 1)));
+  GG_CUDA(cudaMalloc(&scratch, sizeof(uint32_t) * scan_scratch_elems(ncounts)));
+  uint64_t *ka = k0, *kb = k1;
+  uint32_t *va = v0, *vb = v1;
+  int status = GG_OK;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    rs_upsweep<<<(unsigned)ntiles, RS_THREADS, 0, g->stream>>>(ka, n, shift, counts, (uint32_t)ntiles);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = exclusive_scan<uint32_t, ArrayIn<uint32_t>>(ArrayIn<uint32_t>{counts}, ncounts, scanned, scratch,
+                                                      g->stream, nullptr);
+    if (e == cudaSuccess) {
+      rs_scatter<<<(unsigned)ntiles, RS_THREADS, 0, g->stream>>>(ka, va, kb, vb, n, shift, scanned,
+                                                                 (uint32_t)ntiles);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      status = cuda_status(e, "radix sort");
+      break;
+    }
+    uint64_t *tk = ka; ka = kb; kb = tk;
+    uint32_t *tv = va; va = vb; vb = tv;
+  }
+  cudaStreamSynchronize(g->stream);
+  cudaFree(counts);
+  cudaFree(scanned);
+  cudaFree(scratch);
+  *kres = ka;
+  *vres = va;
+  return status;
+}
+
+// ------------------------------------------------------------------ build kernels
+// mode 0: key (src,dst); 1: key (dst,src); 2: both, records then reverses.
+__global__ void make_keys(const uint32_t *__restrict__ rec, size_t E, int words, int mode, int bits, uint32_t V,
+                          uint64_t *__restrict__ keys, uint32_t *__restrict__ vals, unsigned *err) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < E; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t s = rec[i * words], d = rec[i * words + 1];
+    uint32_t wb = words == 3 ? rec[i * words + 2] : 0u;
+    if (s >= V || d >= V) {
+      atomicOr(err, 1u);
+      s = 0;
+      d = 0;
+    }
+    uint64_t fwd = ((uint64_t)s << bits) | d, rev = ((uint64_t)d << bits) | s;
+    if (mode == 0) {
+      keys[i] = fwd;
+    } else if (mode == 1) {
+      keys[i] = rev;
+    } else {
+      keys[i] = fwd;
+      keys[E + i] = rev;
+    }
+    if (vals) {
+      vals[i] = wb;
+      if (mode == 2) vals[E + i] = wb;
+    }
+  }
+}
+
+// off[v] = first position whose major id is >= v, for v in [0, V].
+__global__ void offsets_from_keys(const uint64_t *__restrict__ keys, size_t n, int bits, uint32_t V,
+                                  uint64_t *__restrict__ off, uint32_t *__restrict__ nbr) {
+  const uint64_t mask = (bits >= 64) ? ~0ull : ((1ull << bits) - 1);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint64_t k = keys[i];
+    uint64_t maj = k >> bits;
+    nbr[i] = (uint32_t)(k & mask);
+    long long prev = i ? (long long)(keys[i - 1] >> bits) : -1ll;
+    for (long long v = prev + 1; v <= (long long)maj; v++) off[v] = i;
+    if (i == n - 1)
+      for (uint64_t v = maj + 1; v <= V; v++) off[v] = n;
+  }
+}
+
+__global__ void degrees_from_offsets(const uint64_t *__restrict__ off, uint32_t V, uint32_t *__restrict__ deg) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    deg[v] = (uint32_t)(off[v + 1] - off[v]);
+}
+
+__global__ void collect_hubs(const uint32_t *__restrict__ deg, uint32_t V, uint32_t threshold,
+                             uint32_t *__restrict__ hubs, unsigned *count) {
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t n = ((size_t)V + 31) / 32 * 32;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    bool p = v < V && deg[v] > threshold;
+    queue_push(p, (uint32_t)v, hubs, count);
+  }
+}
+
+__global__ void gen_rmat_kernel(uint32_t *__restrict__ rec, uint64_t E, uint32_t scale, uint64_t key, int weighted) {
+  int words = weighted ? 3 : 2;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t s, d;
+    gg_rmat_edge(key, scale, e, &s, &d);
+    rec[e * words] = s;
+    rec[e * words + 1] = d;
+    if (weighted) rec[e * words + 2] = __float_as_uint(gg_gen_weight(key, e));
+  }
+}
+
+__global__ void gen_grid_kernel(uint32_t *__restrict__ rec, uint64_t E, uint32_t n, uint64_t key, int weighted) {
+  int words = weighted ? 3 : 2;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t s, d;
+    gg_grid_edge(n, e, &s, &d);
+    rec[e * words] = s;
+    rec[e * words + 1] = d;
+    if (weighted) rec[e * words + 2] = __float_as_uint(gg_gen_weight(key, e));
+  }
+}
+
+static int bits_for(uint32_t V) {
+  int b = 1;
+  while (b < 32 && ((uint64_t)1 << b) < V) b++;
+  return b;
+}
+
+// Builds one direction from keys already written by make_keys.
+static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_alt, uint32_t *v_alt, size_t n,
+                     int bits, Dir *d) {
+  uint64_t *ks;
+  uint32_t *vs;
+  GG_TRY(radix_sort(g, keys, vals, k_alt, v_alt, n, 2 * bits, &ks, &vs));
+  uint32_t V = g->V;
+  GG_CUDA(cudaMalloc(&d->off, sizeof(uint64_t) * ((size_t)V + 1)));
+  GG_CUDA(cudaMalloc(&d->nbr, sizeof(uint32_t) * (n ? n : 1)));
+  GG_CUDA(cudaMalloc(&d->deg, sizeof(uint32_t) * ((size_t)V + 1)));
+  g->graph_bytes += sizeof(uint64_t) * ((size_t)V + 1) + sizeof(uint32_t) * (n + (size_t)V + 1);
+  if (n == 0) {
+    GG_CUDA(cudaMemsetAsync(d->off, 0, sizeof(uint64_t) * ((size_t)V + 1), g->stream));
+  } else {
+    offsets_from_keys<<<grid_for(n, 256, g->num_sms, 16), 256, 0, g->stream>>>(ks, n, bits, V, d->off, d->nbr);
+    GG_CUDA(cudaGetLastError());
+  }
+  degrees_from_offsets<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->off, V, d->deg);
+  GG_CUDA(cudaGetLastError());
+  if (g->weighted) {
+    GG_CUDA(cudaMalloc(&d->w, sizeof(float) * (n ? n : 1)));
+    g->graph_bytes += sizeof(float) * n;
+    if (n) GG_CUDA(cudaMemcpyAsync(d->w, vs, sizeof(float) * n, cudaMemcpyDeviceToDevice, g->stream));
+  }
+  // hub list: in-lists longer than the pull kernels' warp-cooperative range
+  unsigned *cnt = nullptr;
+  GG_CUDA(cudaMalloc(&cnt, sizeof(unsigned)));
+  GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned), g->stream));
+  uint32_t *tmp = nullptr;
+  GG_CUDA(cudaMalloc(&tmp, sizeof(uint32_t) * ((size_t)V + 1)));
+  collect_hubs<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->deg, V, g->hub_threshold, tmp, cnt);
+  GG_CUDA(cudaGetLastError());
+  unsigned nh = 0;
+  GG_CUDA(cudaMemcpyAsync(&nh, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  d->nhubs = nh;
+  GG_CUDA(cudaMalloc(&d->hubs, sizeof(uint32_t) * (nh ? nh : 1)));
+  if (nh) GG_CUDA(cudaMemcpyAsync(d->hubs, tmp, sizeof(uint32_t) * nh, cudaMemcpyDeviceToDevice, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  cudaFree(tmp);
+  cudaFree(cnt);
+  g->graph_bytes += sizeof(uint32_t) * nh;
+  return GG_OK;
+}
+
+static void free_dir(Dir *d) {
+  if (d->off) cudaFree(d->off);
+  if (d->nbr) cudaFree(d->nbr);
+  if (d->w) cudaFree(d->w);
+  if (d->deg) cudaFree(d->deg);
+  if (d->hubs) cudaFree(d->hubs);
+  *d = Dir();
+}
+
+void graph_destroy(gg_graph *g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  bool alias = g->in.nbr == g->out.nbr;
+  free_dir(&g->out);
+  if (!alias) free_dir(&g->in);
+  ws_free_all(g);
+  if (g->ev0) cudaEventDestroy(g->ev0);
+  if (g->ev1) cudaEventDestroy(g->ev1);
+  for (cudaEvent_t e : g->evpool) cudaEventDestroy(e);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+static int graph_create(int device, uint32_t V, int weighted, int symmetric, gg_graph **out) {
+  if (V == 0) {
+    set_error("vertices must be > 0");
+    return GG_ERR_INVALID;
+  }
+  int ndev = 0;
+  GG_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) {
+    set_error("device %d out of range (%d devices)", device, ndev);
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(device));
+  gg_graph *g = new gg_graph();
+  g->device = device;
+  g->V = V;
+  g->weighted = weighted ? 1 : 0;
+  g->symmetric = symmetric ? 1 : 0;
+  g->hub_threshold = 1u << 14;
+  cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaMalloc(&g->ws.ctr, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaMallocHost(&g->ws.ctr_host, sizeof(Counters));
+  if (e != cudaSuccess) {
+    graph_destroy(g);
+    return cuda_status(e, "graph create");
+  }
+  *out = g;
+  return GG_OK;
+}
+
+// Builds CSR/CSC from E records in device memory (4-byte aligned).
+static int build_from_device_records(gg_graph *g, const uint32_t *rec, uint64_t E) {
+  int words = g->weighted ? 3 : 2;
+  g->E = E;
+  size_t n = g->symmetric ? 2 * E : E;
+  g->nadj = n;
+  if (n >= 0xFFFFFFFFull) {
+    set_error("%llu adjacency entries per direction: the device sort supports < 2^32",
+              (unsigned long long)n);
+    return GG_ERR_TOO_LARGE;
+  }
+  int bits = bits_for(g->V);
+  uint64_t *k0 = nullptr, *k1 = nullptr;
+  uint32_t *v0 = nullptr, *v1 = nullptr;
+  unsigned *err = nullptr;
+  int status = GG_OK;
+  cudaError_t e = cudaMalloc(&k0, sizeof(uint64_t) * (n ? n : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&k1, sizeof(uint64_t) * (n ? n : 1));
+  if (e == cudaSuccess && g->weighted) e = cudaMalloc(&v0, sizeof(uint32_t) * (n ? n : 1));
+  if (e == cudaSuccess && g->weighted) e = cudaMalloc(&v1, sizeof(uint32_t) * (n ? n : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(unsigned), g->stream);
+  if (e != cudaSuccess) status = cuda_status(e, "build buffers");
+  unsigned blocks = grid_for(E, 256, g->num_sms, 16);
+  for (int pass = 0; status == GG_OK && pass < (g->symmetric ? 1 : 2); pass++) {
+    int mode = g->symmetric ? 2 : pass;
+    if (E) {
+      make_keys<<<blocks, 256, 0, g->stream>>>(rec, E, words, mode, bits, g->V, k0, v0, err);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) {
+        status = cuda_status(e, "make_keys");
+        break;
+      }
+      unsigned herr = 0;
+      e = cudaMemcpyAsync(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+      if (e != cudaSuccess) {
+        status = cuda_status(e, "make_keys");
+        break;
+      }
+      if (herr) {
+        set_error("an edge names a vertex id >= vertices (%u)", g->V);
+        status = GG_ERR_RANGE;
+        break;
+      }
+    }
+    status = build_dir(g, k0, v0, k1, v1, n, bits, pass == 0 ? &g->out : &g->in);
+  }
+  cudaStreamSynchronize(g->stream);
+  cudaFree(k0);
+  cudaFree(k1);
+  if (v0) cudaFree(v0);
+  if (v1) cudaFree(v1);
+  if (err) cudaFree(err);
+  if (status == GG_OK && g->symmetric) g->in = g->out;
+  return status;
+}
+
+static uint64_t unit_of(int weighted) { return weighted ? 12 : 8; }
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+const char *gg_last_error(void) { return g_err; }
+
+int gg_host_alloc(uint64_t bytes, void **out) {
+  if (!out) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaMallocHost(out, bytes ? bytes : 1));
+  return GG_OK;
+}
+
+int gg_host_free(void *p) {
+  if (p) GG_CUDA(cudaFreeHost(p));
+  return GG_OK;
+}
+
+int gg_graph_from_device_records(const void *d_records, uint64_t bytes, uint32_t vertices, int weighted,
+                                 int symmetric, int device, gg_graph **out) {
+  if (!out || (!d_records && bytes >= unit_of(weighted))) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  if ((uintptr_t)d_records % 4) {
+    set_error("device records must be 4-byte aligned");
+    return GG_ERR_INVALID;
+  }
+  gg_graph *g = nullptr;
+  GG_TRY(graph_create(device, vertices, weighted, symmetric, &g));
+  int s = build_from_device_records(g, (const uint32_t *)d_records, bytes / unit_of(weighted));
+  if (s != GG_OK) {
+    graph_destroy(g);
+    return s;
+  }
+  *out = g;
+  return GG_OK;
+}
+
+int gg_graph_from_records(const void *records, uint64_t bytes, uint32_t vertices, int weighted, int symmetric,
+                          int device, gg_graph **out) {
+  uint64_t unit = unit_of(weighted);
+  uint64_t E = bytes / unit;
+  if (!out || (!records && E)) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  gg_graph *g = nullptr;
+  GG_TRY(graph_create(device, vertices, weighted, symmetric, &g));
+  void *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, E * unit ? E * unit : 16);
+  if (e == cudaSuccess && E) e = cudaMemcpy(d, records, E * unit, cudaMemcpyHostToDevice);
+  int s = e == cudaSuccess ? build_from_device_records(g, (const uint32_t *)d, E) : cuda_status(e, "copy records");
+  if (d) cudaFree(d);
+  if (s != GG_OK) {
+    graph_destroy(g);
+    return s;
+  }
+  *out = g;
+  return GG_OK;
+}
+
+int gg_graph_load(const char *path, uint32_t vertices, int weighted, int symmetric, int device, gg_graph **out) {
+  if (!path || !out) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  int fd = open(path, O_RDONLY);
+  if (fd < 0) {
+    set_error("cannot open %s: %s", path, strerror(errno));
+    return GG_ERR_IO;
+  }
+  struct stat st;
+  if (fstat(fd, &st) != 0) {
+    set_error("cannot stat %s: %s", path, strerror(errno));
+    close(fd);
+    return GG_ERR_IO;
+  }
+  uint64_t unit = unit_of(weighted);
+  uint64_t E = (uint64_t)st.st_size / unit;
+  uint64_t total = E * unit;
+  gg_graph *g = nullptr;
+  int s = graph_create(device, vertices, weighted, symmetric, &g);
+  if (s != GG_OK) {
+    close(fd);
+    return s;
+  }
+  // stream the file through two pinned chunks
+  const size_t CH = (size_t)64 << 20;
+  char *pin[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  char *d = nullptr;
+  cudaError_t e = cudaMalloc((void **)&d, total ? total : 16);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    e = cudaMallocHost((void **)&pin[i], CH);
+    if (e == cudaSuccess) e = cudaEventCreate(&done[i]);
+  }
+  if (e != cudaSuccess) s = cuda_status(e, "load buffers");
+  uint64_t off = 0;
+  int k = 0;
+  while (s == GG_OK && off < total) {
+    size_t want = (size_t)((total - off) < CH ? (total - off) : CH);
+    e = cudaEventSynchronize(done[k]);
+    if (e != cudaSuccess) {
+      s = cuda_status(e, "load");
+      break;
+    }
+    size_t got = 0;
+    while (got < want) {
+      ssize_t r = pread(fd, pin[k] + got, want - got, (off_t)(off + got));
+      if (r <= 0) {
+        set_error("read error on %s at %llu", path, (unsigned long long)(off + got));
+        s = GG_ERR_IO;
+        break;
+      }
+      got += (size_t)r;
+    }
+    if (s != GG_OK) break;
+    e = cudaMemcpyAsync(d + off, pin[k], want, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(done[k], g->stream);
+    if (e != cudaSuccess) {
+      s = cuda_status(e, "load copy");
+      break;
+    }
+    off += want;
+    k ^= 1;
+  }
+  close(fd);
+  cudaStreamSynchronize(g->stream);
+  for (int i = 0; i < 2; i++) {
+    if (pin[i]) cudaFreeHost(pin[i]);
+    if (done[i]) cudaEventDestroy(done[i]);
+  }
+  if (s == GG_OK) s = build_from_device_records(g, (const uint32_t *)d, E);
+  if (d) cudaFree(d);
+  if (s != GG_OK) {
+    graph_destroy(g);
+    return s;
+  }
+  *out = g;
+  return GG_OK;
+}
+
+uint64_t gg_generate_count(int kind, uint32_t p1, uint32_t p2) {
+  if (kind == 0) return p1 > 31 ? 0 : ((uint64_t)1 << p1) * p2;
+  if (kind == 1) return gg_grid_count(p1);
+  return 0;
+}
+
+int gg_generate_records(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted, void *records,
+                        int threads) {
+  uint64_t E = gg_generate_count(kind, p1, p2);
+  if ((kind != 0 && kind != 1) || (kind == 0 && (p1 < 1 || p1 > 31)) || (!records && E)) {
+    set_error("bad generator arguments");
+    return GG_ERR_INVALID;
+  }
+  if (threads <= 0) threads = (int)std::thread::hardware_concurrency();
+  if (threads <= 0) threads = 1;
+  uint64_t key = gg_gen_key(seed);
+  int words = weighted ? 3 : 2;
+  uint32_t *rec = (uint32_t *)records;
+  auto work = [&](uint64_t a, uint64_t b) {
+    for (uint64_t e = a; e < b; e++) {
+      uint32_t s, d;
+      if (kind == 0)
+        gg_rmat_edge(key, p1, e, &s, &d);
+      else
+        gg_grid_edge(p1, e, &s, &d);
+      rec[e * words] = s;
+      rec[e * words + 1] = d;
+      if (weighted) {
+        float w = gg_gen_weight(key, e);
+        memcpy(&rec[e * words + 2], &w, 4);
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  uint64_t chunk = (E + threads - 1) / threads;
+  for (int t = 0; t < threads; t++) {
+    uint64_t a = (uint64_t)t * chunk, b = a + chunk < E ? a + chunk : E;
+    if (a >= b) break;
+    pool.emplace_back(work, a, b);
+  }
+  for (auto &th : pool) th.join();
+  return GG_OK;
+}
+
+int gg_graph_generate(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted, int symmetric, int device,
+                      gg_graph **out) {
+  uint64_t E = gg_generate_count(kind, p1, p2);
+  uint32_t V;
+  if (kind == 0 && p1 >= 1 && p1 <= 31) {
+    V = 1u << p1;
+  } else if (kind == 1 && p1 >= 1 && (uint64_t)p1 * p1 < 0xFFFFFFFFull) {
+    V = p1 * p1;
+  } else {
+    set_error("bad generator arguments");
+    return GG_ERR_INVALID;
+  }
+  if (!out) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  gg_graph *g = nullptr;
+  GG_TRY(graph_create(device, V, weighted, symmetric, &g));
+  uint32_t *d = nullptr;
+  int words = weighted ? 3 : 2;
+  cudaError_t e = cudaMalloc(&d, E ? E * words * 4 : 16);
+  uint64_t key = gg_gen_key(seed);
+  if (e == cudaSuccess && E) {
+    unsigned blocks = grid_for(E, 256, g->num_sms, 32);
+    if (kind == 0)
+      gen_rmat_kernel<<<blocks, 256, 0, g->stream>>>(d, E, p1, key, weighted);
+    else
+      gen_grid_kernel<<<blocks, 256, 0, g->stream>>>(d, E, p1, key, weighted);
+    e = cudaGetLastError();
+  }
+  int s = e == cudaSuccess ? build_from_device_records(g, d, E) : cuda_status(e, "generate");
+  if (d) cudaFree(d);
+  if (s != GG_OK) {
+    graph_destroy(g);
+    return s;
+  }
+  *out = g;
+  return GG_OK;
+}
+
+int gg_graph_free(gg_graph *g) {
+  graph_destroy(g);
+  return GG_OK;
+}
+
+int gg_graph_info_get(const gg_graph *g, gg_graph_info *info) {
+  if (!g || !info) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  info->vertices = g->V;
+  info->edges = g->E;
+  info->adj_entries = g->nadj;
+  info->weighted = g->weighted;
+  info->symmetric = g->symmetric;
+  info->transposed = g->transposed;
+  info->device = g->device;
+  uint64_t ws_bytes = 0;
+  for (int i = 0; i < WS_NSLOTS; i++) ws_bytes += g->ws.bytes[i];
+  info->device_bytes = g->graph_bytes + ws_bytes;
+  return GG_OK;
+}
+
+int gg_graph_transpose(gg_graph *g) {
+  if (!g) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  Dir t = g->out;
+  g->out = g->in;
+  g->in = t;
+  g->transposed ^= 1;
+  return GG_OK;
+}
+
+int gg_graph_adjacency(const gg_graph *g, int incoming, uint64_t *offsets, uint32_t *neighbours, float *weights,
+                       uint32_t *degree) {
+  if (!g) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  const Dir &d = incoming ? g->in : g->out;
+  if (offsets) GG_CUDA(cudaMemcpy(offsets, d.off, sizeof(uint64_t) * ((size_t)g->V + 1), cudaMemcpyDeviceToHost));
+  if (neighbours && g->nadj)
+    GG_CUDA(cudaMemcpy(neighbours, d.nbr, sizeof(uint32_t) * g->nadj, cudaMemcpyDeviceToHost));
+  if (weights && g->weighted && g->nadj)
+    GG_CUDA(cudaMemcpy(weights, d.w, sizeof(float) * g->nadj, cudaMemcpyDeviceToHost));
+  if (degree) GG_CUDA(cudaMemcpy(degree, d.deg, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost));
+  return GG_OK;
+}
+
+int gg_is_sparse(uint64_t active_edges, uint64_t edges) { return active_edges < edges / 20 ? 1 : 0; }
+
+const void *gg_result_device_ptr(const gg_graph *g, int which) {
+  if (!g || which < 0 || which > 1) return nullptr;
+  return g->result[which];
+}
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+/*
+ * gemini_gb300.h -- C ABI of the GB300-native Gemini edge-processing engine.
+ *
+ * One graph lives on one GPU.  Every call is synchronous with respect to the
+ * host: when it returns, results requested into host memory are there.
+ * Status codes replace the reference's assert()/exit(-1); nothing in the
+ * library aborts the process.
+ *
+ * Each entry point names the reference interface it replaces
+ * (core/graph.hpp, toolkits/*.cpp of shugo256/GeminiGraph).  Vertex ids are
+ * uint32 (VertexId, core/type.hpp:24), edge counts uint64 (EdgeId,
+ * core/type.hpp:25).  Input records are the reference's binary edge list
+ * (EdgeUnit, core/type.hpp:27-41): packed {uint32 src, uint32 dst} (8 B) or
+ * {uint32 src, uint32 dst, float weight} (12 B); a trailing partial record
+ * is ignored, as core/graph.hpp:782 does.
+ *
+ * Thread safety: calls on different graphs may run from different host
+ * threads; calls on one graph must be serialised by the caller.
+ */
+#ifndef GEMINI_GB300_H
+#define GEMINI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define GG_OK 0
+#define GG_ERR_INVALID 1      /* bad argument (null pointer, root >= vertices, ...) */
+#define GG_ERR_IO 2           /* file missing or unreadable */
+#define GG_ERR_RANGE 3        /* an edge names a vertex id >= vertices */
+#define GG_ERR_CUDA 4         /* CUDA runtime error (no device, launch failure) */
+#define GG_ERR_NOMEM 5        /* device or pinned host allocation failed */
+#define GG_ERR_UNWEIGHTED 6   /* the operation needs edge weights */
+#define GG_ERR_TOO_LARGE 7    /* adjacency entries per direction >= 2^32 */
+#define GG_ERR_LIMIT 8        /* a fixed capacity of the call was exceeded */
+
+typedef struct gg_graph gg_graph;
+
+/* Mirrors the public fields of Graph<EdgeData> (core/graph.hpp:94-111). */
+typedef struct {
+  uint32_t vertices;         /* |V| */
+  uint64_t edges;            /* file records: `edges` of the sparse/dense switch */
+  uint64_t adj_entries;      /* adjacency entries per direction (2*edges if symmetric) */
+  int32_t weighted;          /* 1: float edge data (EdgeData = float) */
+  int32_t symmetric;         /* 1: loaded by load_undirected_from_directed */
+  int32_t transposed;        /* 1: after an odd number of gg_graph_transpose calls */
+  int32_t device;            /* CUDA device ordinal */
+  uint64_t device_bytes;     /* device memory held by the graph and its workspace */
+} gg_graph_info;
+
+/* Per-call record of a traversal: one row per process_edges call. */
+typedef struct {
+  int32_t trace_capacity;    /* in: rows the arrays below can take (0 = no trace) */
+  int32_t calls;             /* out: process_edges calls made */
+  int32_t *mode;             /* in/out: per call, 0 = sparse (push), 1 = dense (pull) */
+  uint64_t *active_edges;    /* in/out: per call, the switch value (graph.hpp:1503-1508) */
+  uint64_t *activated;       /* in/out: per call, vertices the slots activated */
+  double *call_ms;           /* in/out (may be NULL): per call, device time of the call's
+                                edge kernel (push or pull), CUDA events on the graph's stream */
+  uint64_t active_edges_total; /* out: sum of active_edges over all calls (TEPS numerator) */
+  double device_ms;          /* out: device time of the traversal (CUDA events) */
+  int32_t kernel_launches;   /* out: kernels this call launched */
+} gg_run_stats;
+
+/* Last error message of the calling thread ("" when none). */
+const char *gg_last_error(void);
+
+/* Pinned (page-locked) host memory for inputs and results: the
+ * alloc_vertex_array of the host side (core/graph.hpp:229-237). */
+int gg_host_alloc(uint64_t bytes, void **out);
+int gg_host_free(void *p);
+
+/* ---- graph store ---- */
+
+/* Graph::load_directed (core/graph.hpp:772) when symmetric == 0,
+ * Graph::load_undirected_from_directed (core/graph.hpp:350) when 1.
+ * Reads the edge-list file, builds CSR (out) and CSC (in) on the device. */
+int gg_graph_load(const char *path, uint32_t vertices, int weighted, int symmetric,
+                  int device, gg_graph **out);
+
+/* As gg_graph_load, from records already in host memory. */
+int gg_graph_from_records(const void *records, uint64_t bytes, uint32_t vertices,
+                          int weighted, int symmetric, int device, gg_graph **out);
+
+/* As gg_graph_load, from records already in device memory (not modified). */
+int gg_graph_from_device_records(const void *d_records, uint64_t bytes, uint32_t vertices,
+                                 int weighted, int symmetric, int device, gg_graph **out);
+
+/* Builds a graph from a seeded R-MAT (a=.57 b=.19 c=.19 d=.05) or grid edge list
+ * generated on the device; identical to loading the file gg_generate_* writes.
+ * kind 0 = R-MAT (p1 = scale, p2 = edge factor), 1 = grid (p1 = side, p2 unused). */
+int gg_graph_generate(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted,
+                      int symmetric, int device, gg_graph **out);
+
+/* Host generator of the same records (records = edge count * 8 or 12 bytes). */
+uint64_t gg_generate_count(int kind, uint32_t p1, uint32_t p2);
+int gg_generate_records(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted,
+                        void *records, int threads);
+
+/* ~Graph: frees all device memory of the graph. */
+int gg_graph_free(gg_graph *g);
+
+int gg_graph_info_get(const gg_graph *g, gg_graph_info *info);
+
+/* Graph::transpose (core/graph.hpp:760): swaps the two directions. */
+int gg_graph_transpose(gg_graph *g);
+
+/* Copies one direction to host memory (incoming != 0: CSC).  Any pointer may be
+ * NULL.  offsets: vertices+1 entries; neighbours/weights: adj_entries entries;
+ * degree: vertices entries (out_degree / in_degree, core/graph.hpp:110-111). */
+int gg_graph_adjacency(const gg_graph *g, int incoming, uint64_t *offsets, uint32_t *neighbours,
+                       float *weights, uint32_t *degree);
+
+/* ---- toolkits (the compute() of toolkits/*.cpp, on one GPU) ----
+ * Output pointers are host memory; NULL leaves the result on the device
+ * (see gg_result_device_ptr).  stats may be NULL. */
+
+/* toolkits/bfs.cpp:22-109: parent array; parent[v] == vertices if unreached. */
+int gg_bfs(gg_graph *g, uint32_t root, uint32_t *parent, gg_run_stats *stats);
+
+/* toolkits/pagerank.cpp:26-129: double ranks after `iterations` iterations;
+ * deltas (may be NULL) receives the `iterations` values printed as delta(i). */
+int gg_pagerank(gg_graph *g, int iterations, double *ranks, double *deltas, gg_run_stats *stats);
+
+/* As gg_pagerank in float arithmetic (float ranks, float sums). */
+int gg_pagerank_f32(gg_graph *g, int iterations, float *ranks, double *deltas, gg_run_stats *stats);
+
+/* toolkits/cc.cpp:22-88 on a symmetric graph: min-label of every vertex. */
+int gg_cc(gg_graph *g, uint32_t *label, gg_run_stats *stats);
+
+/* toolkits/sssp.cpp:24-90 on a weighted graph: float distances, 1e9 if unreached. */
+int gg_sssp(gg_graph *g, uint32_t root, float *distance, gg_run_stats *stats);
+
+/* toolkits/bc.cpp:24-196 (compute): dependencies and inv_num_paths (1/path count;
+ * inf for unreached vertices, whose dependency is NaN as in the reference). */
+int gg_bc(gg_graph *g, uint32_t root, double *dependencies, double *inv_num_paths,
+          gg_run_stats *stats);
+
+/* Device address of the last result of a toolkit kept on the device:
+ * which = 0 primary output (parent / ranks / label / distance / dependencies),
+ * 1 secondary (inv_num_paths).  Valid until the next toolkit call on g. */
+const void *gg_result_device_ptr(const gg_graph *g, int which);
+
+/* ---- engine primitives ---- */
+
+/* Graph::process_vertices (core/graph.hpp:1406-1469) for the reduction
+ * process_edges makes first: sum of out_degree over the set bits of a host
+ * bitmap in the reference's layout (core/bitmap.hpp: 64-bit words,
+ * vertices/64 + 1 of them). */
+int gg_active_edges(gg_graph *g, const uint64_t *active_bitmap, uint64_t *active_edges);
+
+/* The sparse/dense switch of process_edges (core/graph.hpp:1509). */
+int gg_is_sparse(uint64_t active_edges, uint64_t edges);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,284 @@
+"""GPU parity: the CUDA engine against the CPU oracle (itself pinned to the
+reference's outputs) and against the reference fixtures directly.
+
+Bars (the reference's own determinism, measured): CC labels, SSSP float
+distances and BFS levels bit-exact; BFS parents a valid tree; PageRank and BC
+(double) within relative L1 1e-10 of the oracle (the tolerance the
+comparison states; the float PageRank variant within 1e-5).  The per-call
+trace -- mode, active_edges, activated -- must equal the oracle's exactly:
+that pins the sparse/dense switch (core/graph.hpp:1503-1509).
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import geminigraph_gb300 as gg
+import graphgen
+from golden_util import Fixture, names
+from oracle.oracle import OracleGraph, bfs_levels
+
+pytestmark = pytest.mark.gpu
+
+PR_TOL = 1e-10
+PR_F32_TOL = 1e-5
+BC_TOL = 1e-10
+
+
+def rel_l1(a, b):
+    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+
+def check_parent_tree(parent, root, V, src, dst):
+    lv = bfs_levels(parent, root)
+    reached = np.nonzero(parent < V)[0]
+    edges = set(zip(src.tolist(), dst.tolist()))
+    for v in reached:
+        if v != root:
+            assert (int(parent[v]), int(v)) in edges
+    return lv
+
+
+def random_graph(V, E, seed, selfloops=True):
+    rng = np.random.default_rng(seed)
+    s = rng.integers(0, V, E).astype(np.uint32)
+    d = rng.integers(0, V, E).astype(np.uint32)
+    if not selfloops:
+        d = np.where(d == s, (d + 1) % V, d).astype(np.uint32)
+    w = graphgen.weights(seed, np.arange(E, dtype=np.uint64))
+    return s, d, w
+
+
+CASES = {}
+
+
+def case(name):
+    if name in CASES:
+        return CASES[name]
+    if name.startswith("golden:"):
+        fx = Fixture(name.split(":")[1])
+        c = (fx.V, fx.src, fx.dst, fx.w, fx.root)
+    elif name == "rmat16":
+        s, d, w = graphgen.rmat(16, 16, 3, weighted=True)
+        c = (1 << 16, s, d, w, None)
+    elif name == "grid128":
+        s, d, w = graphgen.grid(128, seed=2, weighted=True)
+        c = (128 * 128, s, d, w, 0)
+    elif name == "random_odd":
+        s, d, w = random_graph(777, 5000, 11)
+        c = (777, s, d, w, None)
+    elif name == "chain":
+        V = 300
+        s = np.arange(V - 1, dtype=np.uint32)
+        d = s + 1
+        w = np.full(V - 1, 0.5, np.float32)
+        c = (V, s, d, w, 0)
+    elif name == "star":
+        V = 5000
+        s = np.zeros(V - 1, np.uint32)
+        d = np.arange(1, V, dtype=np.uint32)
+        s = np.concatenate([s, d[:100]])
+        d = np.concatenate([d, np.zeros(100, np.uint32)])
+        w = graphgen.weights(4, np.arange(len(s), dtype=np.uint64))
+        c = (V, s.astype(np.uint32), d.astype(np.uint32), w, 0)
+    else:
+        raise KeyError(name)
+    V, s, d, w, root = c
+    if root is None:
+        root = graphgen.pick_root(s, V, seed=V)
+    CASES[name] = (V, s, d, w, root)
+    return CASES[name]
+
+
+ALL = ["golden:" + n for n in names()] + ["rmat16", "grid128", "random_odd", "chain", "star"]
+
+
+@pytest.fixture(scope="module", params=ALL)
+def gcase(request):
+    return request.param, case(request.param)
+
+
+def test_adjacency_matches_oracle(gcase):
+    _, (V, s, d, w, _) = gcase
+    for symmetric in (False, True):
+        g = gg.Graph.from_edges(V, s, d, w, symmetric=symmetric)
+        o = OracleGraph(V, s, d, w, symmetric=symmetric)
+        for incoming in (False, True):
+            go, gn, gw, gd = g.adjacency(incoming)
+            oo, on, ow, od = o.adjacency(incoming)
+            assert np.array_equal(go, oo)
+            assert np.array_equal(gn, on)
+            assert np.array_equal(gw.view(np.uint32), ow.view(np.uint32))
+            assert np.array_equal(gd, od)
+        info = g.info()
+        assert info["edges"] == len(s)
+        assert info["adj_entries"] == (2 if symmetric else 1) * len(s)
+
+
+def test_bfs(gcase):
+    name, (V, s, d, w, root) = gcase
+    g = gg.Graph.from_edges(V, s, d)
+    parent, st = g.bfs(root)
+    o = OracleGraph(V, s, d)
+    oparent, otrace = o.bfs(root)
+    assert st.rows() == otrace
+    lv = check_parent_tree(parent, root, V, s, d)
+    assert np.array_equal(lv, bfs_levels(oparent, root))
+    assert st.active_edges_total == sum(r[1] for r in otrace)
+    if name.startswith("golden:"):
+        fx = Fixture(name.split(":")[1])
+        assert np.array_equal(lv, bfs_levels(fx["bfs_parent"], root))
+
+
+def test_pagerank(gcase):
+    name, (V, s, d, w, _) = gcase
+    g = gg.Graph.from_edges(V, s, d)
+    ranks, deltas, st = g.pagerank(20)
+    o = OracleGraph(V, s, d)
+    oranks, odeltas, otrace = o.pagerank(20)
+    assert rel_l1(ranks, oranks) < PR_TOL
+    assert np.allclose(deltas, odeltas, rtol=1e-9, atol=1e-15)
+    assert st.rows() == otrace
+    r32, _, _ = g.pagerank(20, f32=True)
+    assert rel_l1(r32.astype(np.float64), oranks) < PR_F32_TOL
+    if name.startswith("golden:"):
+        fx = Fixture(name.split(":")[1])
+        assert rel_l1(ranks, fx["pr_ranks"]) < PR_TOL
+
+
+def test_cc(gcase):
+    name, (V, s, d, w, _) = gcase
+    g = gg.Graph.from_edges(V, s, d, symmetric=True)
+    label, st = g.cc()
+    o = OracleGraph(V, s, d, symmetric=True)
+    olabel, otrace = o.cc()
+    assert np.array_equal(label, olabel)
+    assert st.rows() == otrace
+    if name.startswith("golden:"):
+        assert np.array_equal(label, Fixture(name.split(":")[1])["cc_label"])
+
+
+def test_sssp(gcase):
+    name, (V, s, d, w, root) = gcase
+    g = gg.Graph.from_edges(V, s, d, w)
+    dist, st = g.sssp(root)
+    o = OracleGraph(V, s, d, w)
+    odist, otrace = o.sssp(root)
+    assert np.array_equal(dist.view(np.uint32), odist.view(np.uint32))
+    assert st.rows() == otrace
+    if name.startswith("golden:"):
+        ref = Fixture(name.split(":")[1])["sssp_dist"]
+        assert np.array_equal(dist.view(np.uint32), ref.view(np.uint32))
+
+
+def test_bc(gcase):
+    name, (V, s, d, w, root) = gcase
+    g = gg.Graph.from_edges(V, s, d)
+    dep, inv, st = g.bc(root)
+    o = OracleGraph(V, s, d)
+    odep, oinv, otrace = o.bc(root)
+    assert np.array_equal(np.isnan(dep), np.isnan(odep))
+    assert np.array_equal(inv, oinv)
+    ok = ~np.isnan(odep)
+    assert rel_l1(dep[ok], odep[ok]) < BC_TOL
+    assert [r[:2] for r in st.rows()] == [r[:2] for r in otrace]
+    if name.startswith("golden:"):
+        fx = Fixture(name.split(":")[1])
+        assert np.array_equal(np.isnan(dep), np.isnan(fx["bc_dep"]))
+        assert rel_l1(dep[ok], fx["bc_dep"][ok]) < BC_TOL
+
+
+def test_file_load_matches_records(tmp_path):
+    V, s, d, w, root = case("golden:edgecase")
+    rec = graphgen.to_records(s, d, w) + b"\x01\x02\x03"   # trailing partial record ignored
+    p = tmp_path / "g.wbin"
+    p.write_bytes(rec)
+    g1 = gg.Graph.load(str(p), V, weighted=True)
+    g2 = gg.Graph.from_edges(V, s, d, w)
+    assert g1.info()["edges"] == len(s)
+    for incoming in (False, True):
+        a, b = g1.adjacency(incoming), g2.adjacency(incoming)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_device_generator_matches_host():
+    for kind, p1, p2, wtd in ((gg.RMAT, 12, 8, True), (gg.GRID, 40, 0, True), (gg.RMAT, 10, 16, False)):
+        gd = gg.Graph.generate(kind, p1, p2, 9, weighted=wtd)
+        rec = gg.generate_records(kind, p1, p2, 9, weighted=wtd)
+        V = (1 << p1) if kind == gg.RMAT else p1 * p1
+        gh = gg.Graph.from_records(rec, V, weighted=wtd)
+        for incoming in (False, True):
+            a, b = gd.adjacency(incoming), gh.adjacency(incoming)
+            for x, y in zip(a, b):
+                if x is not None:
+                    assert np.array_equal(x, y)
+
+
+def test_errors():
+    with pytest.raises(gg.GeminiError) as e:
+        gg.Graph.from_edges(10, np.array([1, 12], np.uint32), np.array([2, 3], np.uint32))
+    assert e.value.code == 3
+    g = gg.Graph.from_edges(10, np.array([1, 2], np.uint32), np.array([2, 3], np.uint32))
+    with pytest.raises(gg.GeminiError) as e:
+        g.bfs(10)
+    assert e.value.code == 1
+    with pytest.raises(gg.GeminiError) as e:
+        g.sssp(0)
+    assert e.value.code == 6
+    with pytest.raises(gg.GeminiError) as e:
+        gg.Graph.load("/nonexistent/g.bin", 10)
+    assert e.value.code == 2
+
+
+def test_empty_and_isolated():
+    # no edges at all: every toolkit terminates after one call
+    g = gg.Graph.from_edges(70, np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0, np.float32))
+    parent, st = g.bfs(5)
+    assert parent[5] == 5 and (parent == 70).sum() == 69
+    assert st.calls == 1
+    dist, _ = g.sssp(3)
+    assert dist[3] == 0 and (dist == np.float32(1e9)).sum() == 69
+    ranks, _, _ = g.pagerank(3)
+    assert np.allclose(ranks, 0.15)
+    dep, inv, _ = g.bc(1)
+    assert inv[1] == 1.0 and np.isinf(inv).sum() == 69
+    gs = gg.Graph.from_edges(70, np.zeros(0, np.uint32), np.zeros(0, np.uint32), symmetric=True)
+    label, _ = gs.cc()
+    assert np.array_equal(label, np.arange(70))
+
+
+def test_transpose_roundtrip():
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d)
+    out0 = g.adjacency(False)
+    g.transpose()
+    assert np.array_equal(g.adjacency(True)[1], out0[1])
+    # BFS on the transposed graph follows in-edges
+    parent, _ = g.bfs(root)
+    o = OracleGraph(V, d, s)
+    op, _ = o.bfs(root)
+    assert np.array_equal(bfs_levels(parent, root), bfs_levels(op, root))
+    g.transpose()
+    assert g.info()["transposed"] == 0
+
+
+def test_active_edges_primitive():
+    V, s, d, w, _ = case("random_odd")
+    g = gg.Graph.from_edges(V, s, d)
+    rng = np.random.default_rng(0)
+    words = V // 64 + 1
+    bm = rng.integers(0, 2 ** 63, words, dtype=np.uint64) | (rng.integers(0, 2, words, dtype=np.uint64) << 63)
+    bits = np.unpackbits(bm.view(np.uint8), bitorder="little")[:V].astype(bool)
+    deg = np.bincount(s, minlength=V)
+    assert g.active_edges(bm) == int(deg[bits].sum())
+
+
+def test_repeated_runs_are_stable():
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d, w)
+    d1, _ = g.sssp(root)
+    g.bfs(root)
+    d2, _ = g.sssp(root)
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))

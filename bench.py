@@ -1,0 +1,491 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 edge-processing engine (one JSON line on stdout).
+
+Default workload: BFS (toolkits/bfs.cpp semantics) from seeded non-isolated
+roots on a directed R-MAT graph of scale 26, edge factor 16 (67,108,864
+vertices, 1,073,741,824 edges, a=.57 b=.19 c=.19 d=.05), generated on the
+device from a seed -- synthetic data of the benchmark's shape.  One step =
+one BFS from the next root.  GTEPS = sum over process_edges calls of
+active_edges (core/graph.hpp:1503-1508, identical for the reference and this
+engine) / time.
+
+  value      graph and root resident in HBM; device time of each BFS
+             (CUDA events on the library's stream), results left on device
+  e2e        the same BFS through the C ABI with the parent array copied back
+             to pinned host memory inside the timed region (wall clock)
+  roofline   the dominant edge kernel's algorithmic bytes / its event time
+  cpu_baseline  the reference's own BFS (oracle/_ref, built from the
+             reference sources) on this host's cores on a bounded R-MAT
+             sample; the oracle port when the reference could not be built
+
+--impl reference runs the reference arm: the reference's own CPU BFS on the
+same sample, printed with impl=reference.  Multi-GPU (torchrun): replicas --
+each rank runs its own BFSes on its own GPU; value = all ranks' edges / the
+slowest rank's time.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "GTEPS at RMAT-26 vs HBM roofline; batched BFS/SSSP queries/s, p99 vs plain"
+SEED = 1
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    "bfs": dict(kind="rmat", scale=26, ef=16, weighted=False, symmetric=False,
+                desc="BFS from seeded non-isolated roots on directed R-MAT scale 26, edge factor 16"),
+    "cc": dict(kind="rmat", scale=26, ef=16, weighted=False, symmetric=True,
+               desc="CC (min-label, symmetrised edges) on R-MAT scale 26, edge factor 16"),
+    "pagerank": dict(kind="rmat", scale=20, ef=16, weighted=False, symmetric=False,
+                     desc="PageRank 20 iterations (double) on directed R-MAT scale 20, edge factor 16"),
+    "sssp": dict(kind="rmat", scale=25, ef=16, weighted=True, symmetric=False,
+                 desc="SSSP (float weights in [0,1)) from seeded roots on R-MAT scale 25, edge factor 16"),
+    "bc": dict(kind="rmat", scale=25, ef=16, weighted=False, symmetric=False,
+               desc="BC (double) from seeded roots on R-MAT scale 25, edge factor 16"),
+    "bfs_grid": dict(kind="grid", scale=8192, ef=0, weighted=False, symmetric=False,
+                     desc="BFS on the 8192 x 8192 4-neighbour grid (both directions)"),
+}
+REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs"}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------- distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[1]), sm_max=float(parts[2]), power=float(parts[3]),
+                                 hw=parts[5], hwt=parts[6], swt=parts[7], swp=parts[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        reasons = []
+        for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                          ("swp", "sw_power_cap")):
+            if any(r[key].lower().startswith("active") for r in rows):
+                reasons.append(name)
+        load = [r["sm"] for r in rows]
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(r["sm_max"] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r["power"] for r in rows)}
+
+
+# ----------------------------------------------------------------- helpers
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        d = json.load(open(p))
+        e = d[workload][kernel]
+        return float(e["bytes_per_launch"])
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
+
+
+def algorithmic_bytes(mode, ae, V, n_frontier, workload):
+    """Bytes a call must move (per counted edge: neighbour id + the value it
+    gathers or scatters; per vertex: offsets, degree, state; bitmaps)."""
+    per_edge = {"bfs": 8, "bfs_grid": 8, "cc": 8, "sssp": 12, "bc": 12, "pagerank": 12}[workload]
+    state = {"bfs": 4, "bfs_grid": 4, "cc": 4, "sssp": 4, "bc": 8, "pagerank": 8}[workload]
+    if mode == 1:   # pull: every vertex's offsets, its state write, three bitmaps
+        return per_edge * ae + V * (8 + state) + 3 * (V // 8)
+    return per_edge * ae + n_frontier * (8 + 4 + 4)   # push: frontier offsets, degree, queue entry
+
+
+def make_graph(gg, w, device):
+    if w["kind"] == "rmat":
+        return gg.Graph.generate(gg.RMAT, w["scale"], w["ef"], SEED, weighted=w["weighted"],
+                                 symmetric=w["symmetric"], device=device)
+    return gg.Graph.generate(gg.GRID, w["scale"], 0, SEED, weighted=w["weighted"], symmetric=w["symmetric"],
+                             device=device)
+
+
+def run_once(gg, g, workload, arg, to_host, stats_cls):
+    if workload in ("bfs", "bfs_grid"):
+        _, st = g.bfs(arg, to_host=to_host)
+    elif workload == "cc":
+        _, st = g.cc(to_host=to_host)
+    elif workload == "pagerank":
+        _, _, st = g.pagerank(arg, to_host=to_host)
+    elif workload == "sssp":
+        _, st = g.sssp(arg, to_host=to_host)
+    else:
+        _, _, st = g.bc(arg, to_host=to_host)
+    return st
+
+
+def step_args(gg, g, workload, count):
+    if workload == "pagerank":
+        return [20] * count
+    if workload == "cc":
+        return [None] * count
+    if workload == "bfs_grid":
+        return [0] * count
+    return gg.pick_roots(g.out_degree(), count, seed=SEED + 1000)
+
+
+# ----------------------------------------------------------------- CPU side
+def ref_sample_scale(workload):
+    return {"bfs": 22, "cc": 21, "pagerank": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024}[workload]
+
+
+def cpu_reference(gg, workload, nsteps, warmup):
+    """Times the reference's own compute() (oracle/_ref/bin/ref_<app>) on a
+    bounded sample of the workload; falls back to the oracle port."""
+    from oracle.oracle import OracleGraph
+    w = WORKLOADS[workload]
+    s = ref_sample_scale(workload)
+    if w["kind"] == "rmat":
+        V = 1 << s
+        rec = gg.generate_records(gg.RMAT, s, w["ef"], SEED, weighted=w["weighted"])
+        sample = f"R-MAT scale {s}, edge factor {w['ef']}, seed {SEED}"
+    else:
+        V = s * s
+        rec = gg.generate_records(gg.GRID, s, 0, SEED, weighted=w["weighted"])
+        sample = f"{s} x {s} grid"
+    unit = 12 if w["weighted"] else 8
+    words = rec.view(np.uint32).reshape(-1, unit // 4)
+    src, dst = words[:, 0].copy(), words[:, 1].copy()
+    wts = words[:, 2].view(np.float32).copy() if w["weighted"] else None
+    n = warmup + nsteps
+    if workload in ("bfs", "sssp", "bc"):
+        args = gg.pick_roots(np.bincount(src, minlength=V), n, seed=SEED + 2000)
+    elif workload == "bfs_grid":
+        args = [0] * n
+    elif workload == "pagerank":
+        args = [20] * n
+    else:
+        args = [0] * n
+    # TEPS numerators from the oracle's trace (the same quantity the reference counts)
+    og = OracleGraph(V, src, dst, wts, symmetric=w["symmetric"])
+    numer = []
+    for a in args:
+        if workload in ("bfs", "bfs_grid"):
+            tr = og.bfs(a)[1]
+        elif workload == "sssp":
+            tr = og.sssp(a)[1]
+        elif workload == "bc":
+            tr = og.bc(a)[2]
+        elif workload == "pagerank":
+            tr = og.pagerank(a)[2]
+        else:
+            tr = og.cc()[1]
+        numer.append(sum(r[1] for r in tr))
+    exe = os.path.join(REPO, "oracle", "_ref", "bin", "ref_" + REF_APP[workload])
+    cores = os.cpu_count() or 1
+    if os.path.exists(exe):
+        fd, path = tempfile.mkstemp(suffix=".bin")
+        with os.fdopen(fd, "wb") as f:
+            f.write(rec.tobytes())
+        env = dict(os.environ, OMP_NUM_THREADS=str(cores), GG_REF_THREADS=str(cores))
+        try:
+            p = subprocess.run([exe, path, str(V)] + [str(a) for a in args], capture_output=True, text=True,
+                               env=env, timeout=900)
+        finally:
+            os.unlink(path)
+        times = [float(x) for x in re.findall(r"exec_time=([0-9.]+)", p.stdout)]
+        if p.returncode == 0 and len(times) == n:
+            t = times[warmup:]
+            e = numer[warmup:]
+            return dict(value=sum(e) / sum(t) / 1e9, unit="GTEPS", cores=cores, kind="reference",
+                        sample=f"{sample}; {nsteps} timed runs after {warmup} warm-up; reference compute() "
+                               f"exec_time, {cores} OpenMP threads", times=t, edges=e)
+        log("reference driver failed:", p.returncode, p.stderr[-500:])
+    # oracle port: serial C restatement
+    t, e = [], []
+    for i, a in enumerate(args):
+        t0 = time.perf_counter()
+        if workload in ("bfs", "bfs_grid"):
+            og.bfs(a)
+        elif workload == "sssp":
+            og.sssp(a)
+        elif workload == "bc":
+            og.bc(a)
+        elif workload == "pagerank":
+            og.pagerank(a)
+        else:
+            og.cc()
+        if i >= warmup:
+            t.append(time.perf_counter() - t0)
+            e.append(numer[i])
+    return dict(value=sum(e) / sum(t) / 1e9, unit="GTEPS", cores=1, kind="port",
+                sample=f"{sample}; {nsteps} timed runs after {warmup} warm-up; oracle port, 1 thread",
+                times=t, edges=e)
+
+
+# ----------------------------------------------------------------- arms
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return 0
+    import geminigraph_gb300 as gg
+    w = WORKLOADS[args.workload]
+    r = cpu_reference(gg, args.workload, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(r["value"], 4), "unit": "GTEPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * sum(r["times"]) / len(r["times"]), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f64"}.get(args.workload, "u32"),
+        "data": "synthetic", "config": {"workload": w["desc"], "sample": r["sample"]},
+        "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": round(r["value"], 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gpu_arm(args, dist):
+    import geminigraph_gb300 as gg
+    w = WORKLOADS[args.workload]
+    device = dist.local_rank
+    t0 = time.perf_counter()
+    g = make_graph(gg, w, device)
+    build_s = time.perf_counter() - t0
+    info = g.info()
+    V = info["vertices"]
+    n = args.warmup + args.steps
+    step_in = step_args(gg, g, args.workload, n + args.steps)
+    for a in step_in[:args.warmup]:
+        run_once(gg, g, args.workload, a, False, None)
+    # ---- value: resident inputs, results on device, device time per step
+    clocks = ClockSampler(device)
+    clocks.start()
+    dist.barrier()
+    stats = []
+    wall0 = time.perf_counter()
+    for a in step_in[args.warmup:n]:
+        st = gg.RunStats()
+        st.enable_call_timing()
+        stats.append(run_once_stats(gg, g, args.workload, a, st))
+    wall = time.perf_counter() - wall0
+    dist.barrier()
+    clk = clocks.stop()
+    dev_ms = sum(s.device_ms for s in stats)
+    edges = sum(s.active_edges_total for s in stats)
+    launches = sum(s.kernel_launches for s in stats)
+    t_max = dist.max(dev_ms / 1000.0)
+    edges_all = dist.sum(edges)
+    value = edges_all / t_max / 1e9
+    # ---- dominant kernel roofline
+    per_mode = {0: [0.0, 0.0, 0], 1: [0.0, 0.0, 0]}   # ms, bytes, launches
+    for s in stats:
+        prev_act = 1
+        for i, (mode, ae, act) in enumerate(s.rows()):
+            ms = float(s.call_ms[i])
+            frontier = prev_act if i else 1
+            per_mode[mode][0] += ms
+            per_mode[mode][1] += algorithmic_bytes(mode, ae, V, frontier, args.workload)
+            per_mode[mode][2] += 1
+            prev_act = act
+    dom = 1 if per_mode[1][0] >= per_mode[0][0] else 0
+    kname = {0: "push_lb", 1: "bfs_pull" if args.workload.startswith("bfs") else "pull_reduce"}[dom]
+    peak, peak_kind = peaks()
+    ach = per_mode[dom][1] / (per_mode[dom][0] / 1000.0) / 1e9 if per_mode[dom][0] > 0 else 0.0
+    traffic = committed_traffic(kname, args.workload)
+    total_kernel_ms = per_mode[0][0] + per_mode[1][0]
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": traffic, "launches": per_mode[dom][2],
+                "avg_launch_ms": round(per_mode[dom][0] / max(per_mode[dom][2], 1), 4),
+                "share_of_edge_kernel_time": round(per_mode[dom][0] / total_kernel_ms, 4) if total_kernel_ms else None}
+    # ---- e2e through the C ABI with host buffers
+    host_out = gg.PinnedArray(V, np.uint32 if args.workload in ("bfs", "bfs_grid", "cc") else
+                              (np.float32 if args.workload == "sssp" else np.float64))
+    dist.barrier()
+    e_edges, e_wall = 0, 0.0
+    for a in step_in[n:n + args.steps]:
+        t1 = time.perf_counter()
+        st = run_e2e(gg, g, args.workload, a, host_out)
+        e_wall += time.perf_counter() - t1
+        e_edges += st.active_edges_total
+    e_max = dist.max(e_wall)
+    e_value = dist.sum(e_edges) / e_max / 1e9
+    d2h = V * host_out.itemsize * (2 if args.workload == "bc" else 1)
+    h2d = 4 if args.workload in ("bfs", "bfs_grid", "sssp", "bc") else 0
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_max * 1000 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f64"}.get(args.workload, "u32"),
+        "data": "synthetic (seeded R-MAT / grid generated on the device)",
+        "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"],
+                   "l2": "inputs larger than L2 (graph %.1f GB)" % (info["device_bytes"] / 1e9),
+                   "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
+                   "active_edges_per_step": edges // max(len(stats), 1)},
+        "e2e": {"value": round(e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(e_max * 1000 / args.steps, 3)},
+        "roofline": roofline,
+        "gpu_launches": launches,
+        "wall_s": round(wall, 3),
+        "clocks": clk,
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        try:
+            r = cpu_reference(gg, args.workload, 5, 1)
+            line["cpu_baseline"] = {k: (round(r[k], 4) if k == "value" else r[k])
+                                    for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    return 0
+
+
+def run_once_stats(gg, g, workload, a, st):
+    L = gg.library()
+    import ctypes
+    if workload in ("bfs", "bfs_grid"):
+        gg._check(L.gg_bfs(g.h, a, None, ctypes.byref(st.s)))
+    elif workload == "cc":
+        gg._check(L.gg_cc(g.h, None, ctypes.byref(st.s)))
+    elif workload == "pagerank":
+        gg._check(L.gg_pagerank(g.h, a, None, None, ctypes.byref(st.s)))
+    elif workload == "sssp":
+        gg._check(L.gg_sssp(g.h, a, None, ctypes.byref(st.s)))
+    else:
+        gg._check(L.gg_bc(g.h, a, None, None, ctypes.byref(st.s)))
+    return st
+
+
+def run_e2e(gg, g, workload, a, out):
+    L = gg.library()
+    import ctypes
+    st = gg.RunStats()
+    p = out.ptr
+    if workload in ("bfs", "bfs_grid"):
+        gg._check(L.gg_bfs(g.h, a, p, ctypes.byref(st.s)))
+    elif workload == "cc":
+        gg._check(L.gg_cc(g.h, p, ctypes.byref(st.s)))
+    elif workload == "pagerank":
+        gg._check(L.gg_pagerank(g.h, a, p, None, ctypes.byref(st.s)))
+    elif workload == "sssp":
+        gg._check(L.gg_sssp(g.h, a, p, ctypes.byref(st.s)))
+    else:
+        gg._check(L.gg_bc(g.h, a, p, out.ptr2, ctypes.byref(st.s)))
+    return st
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bfs", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=int, default=None, help="override the workload's R-MAT scale / grid side")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3 (timing rule)")
+        args.warmup = 3
+    if args.scale is not None:
+        WORKLOADS[args.workload] = dict(WORKLOADS[args.workload], scale=args.scale)
+        w = WORKLOADS[args.workload]
+        WORKLOADS[args.workload]["desc"] = w["desc"].replace("scale 26", f"scale {args.scale}").replace(
+            "scale 25", f"scale {args.scale}").replace("scale 20", f"scale {args.scale}")
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return reference_arm(args, dist)
+        return gpu_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

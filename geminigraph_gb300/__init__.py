@@ -40,7 +40,7 @@ class _Info(ctypes.Structure):
 class _Stats(ctypes.Structure):
     _fields_ = [("trace_capacity", ctypes.c_int32), ("calls", ctypes.c_int32),
                 ("mode", ctypes.c_void_p), ("active_edges", ctypes.c_void_p), ("activated", ctypes.c_void_p),
-                ("active_edges_total", ctypes.c_uint64), ("device_ms", ctypes.c_double),
+                ("call_ms", ctypes.c_void_p), ("active_edges_total", ctypes.c_uint64), ("device_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int32)]
 
 
@@ -56,6 +56,8 @@ def library():
     pg = ctypes.POINTER(vp)
     sig = {
         "gg_last_error": ([], ctypes.c_char_p),
+        "gg_host_alloc": ([u64, ctypes.POINTER(vp)], i32),
+        "gg_host_free": ([vp], i32),
         "gg_graph_load": ([ctypes.c_char_p, u32, i32, i32, i32, pg], i32),
         "gg_graph_from_records": ([vp, u64, u32, i32, i32, i32, pg], i32),
         "gg_graph_from_device_records": ([vp, u64, u32, i32, i32, i32, pg], i32),
@@ -101,8 +103,15 @@ class RunStats:
         self.mode = np.zeros(capacity, np.int32)
         self.active_edges = np.zeros(capacity, np.uint64)
         self.activated = np.zeros(capacity, np.uint64)
+        self.call_ms = None
         self.s = _Stats(capacity, 0, self.mode.ctypes.data, self.active_edges.ctypes.data,
-                        self.activated.ctypes.data, 0, 0.0, 0)
+                        self.activated.ctypes.data, None, 0, 0.0, 0)
+
+    def enable_call_timing(self):
+        """Ask for the device time of each call's edge kernel (CUDA events)."""
+        self.call_ms = np.zeros(len(self.mode), np.float64)
+        self.s.call_ms = self.call_ms.ctypes.data
+        return self
 
     @property
     def calls(self):
@@ -123,6 +132,33 @@ class RunStats:
     def rows(self):
         n = min(self.s.calls, len(self.mode))
         return [(int(self.mode[i]), int(self.active_edges[i]), int(self.activated[i])) for i in range(n)]
+
+
+class PinnedArray:
+    """A page-locked host array (gg_host_alloc) of n elements of dtype, and
+    an optional second one of the same size (ptr2)."""
+
+    def __init__(self, n, dtype, second=True):
+        self.dtype = np.dtype(dtype)
+        self.itemsize = self.dtype.itemsize
+        self.n = n
+        self._p = [ctypes.c_void_p(), ctypes.c_void_p()]
+        for i in range(2 if second else 1):
+            _check(library().gg_host_alloc(n * self.itemsize, ctypes.byref(self._p[i])))
+        self.ptr = self._p[0]
+        self.ptr2 = self._p[1] if second else None
+
+    def array(self, which=0):
+        buf = (ctypes.c_char * (self.n * self.itemsize)).from_address(self._p[which].value)
+        return np.frombuffer(buf, self.dtype)
+
+    def __del__(self):
+        try:
+            for p in self._p:
+                if p:
+                    library().gg_host_free(p)
+        except Exception:
+            pass
 
 
 def generate_records(kind, p1, p2, seed, weighted=False, threads=0):
@@ -219,7 +255,9 @@ class Graph:
         return off, nbr[:n], (None if w is None else w[:n]), deg
 
     def out_degree(self):
-        return self.adjacency(False)[3]
+        deg = np.zeros(self.vertices, np.uint32)
+        _check(library().gg_graph_adjacency(self.h, 0, None, None, None, _ptr(deg)))
+        return deg
 
     def active_edges(self, bitmap64):
         out = ctypes.c_uint64()

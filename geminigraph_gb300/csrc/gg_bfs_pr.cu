@@ -4,8 +4,6 @@
 
 namespace gg {
 
-constexpr uint32_t PULL_SMALL = 32;
-
 // ------------------------------------------------------------------ BFS
 // Sparse slot (bfs.cpp:49-59): claim unvisited dst with a CAS on its parent.
 struct BfsPush {
@@ -84,9 +82,8 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
       }
     } else {
       GG_TRY(tr.kbegin());
-      bfs_pull<<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL, bm[cur], parent, a, ctr);
+      GG_TRY(L.bfs_pull(g->in, bm[cur], parent, a, ctr));
       GG_TRY(tr.kend());
-      L.launches += 1;
     }
     GG_CUDA(cudaGetLastError());
     GG_TRY(counters_read(g, &c));
@@ -193,10 +190,8 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
     tr.add(ae < g->E / 20 ? 0 : 1, ae, V);
     PrPull<T> op{buf[cur], buf[cur ^ 1], g->out.deg, i == iterations - 1};
     GG_TRY(tr.kbegin());
-    pull_reduce<PrPull<T>><<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL, op, ActOut(),
-                                                                   per_iter + i);
+    GG_TRY(L.pull(g->in, op, ActOut(), per_iter + i));
     GG_TRY(tr.kend());
-    L.launches += 1;
     GG_CUDA(cudaGetLastError());
     cur ^= 1;
   }

@@ -6,8 +6,6 @@
 
 namespace gg {
 
-constexpr uint32_t PULL_SMALL_R = 32;
-
 // ------------------------------------------------------------------ CC
 // Sparse slot (cc.cpp:48-59): msg = label of the source at the start of the
 // call (snapshot); a lower msg lowers label[dst] and activates dst.
@@ -136,10 +134,8 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
       }
     } else {
       GG_TRY(tr.kbegin());
-      pull_reduce<PullOp><<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL_R, PullOp{cur, nxt}, a,
-                                                                  ctr);
+      GG_TRY(L.pull(g->in, PullOp{cur, nxt}, a, ctr));
       GG_TRY(tr.kend());
-      L.launches += 1;
       T *t = cur;
       cur = nxt;
       nxt = t;
@@ -403,10 +399,8 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
       }
     } else {
       GG_TRY(tr.kbegin());
-      pull_reduce<BcFwdPull><<<L.pull_grid(), PULL_THREADS, 0, s>>>(g->in, V, PULL_SMALL_R,
-                                                                     BcFwdPull{np, bm[cur], visited}, a, ctr);
+      GG_TRY(L.pull(g->in, BcFwdPull{np, bm[cur], visited}, a, ctr));
       GG_TRY(tr.kend());
-      L.launches += 1;
     }
     GG_CUDA(cudaGetLastError());
     GG_TRY(counters_read(g, &c));
@@ -447,10 +441,9 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
       GG_CUDA(cudaMemsetAsync(lvbm, 0, words * 4, s));
       if (ln) bitmap_from_queue<<<grid_for(ln, 256, g->num_sms), 256, 0, s>>>(ql, ln, lvbm);
       GG_TRY(tr.kbegin());
-      pull_reduce<BcBwdPull><<<L.pull_grid(), PULL_THREADS, 0, s>>>(tin, V, PULL_SMALL_R,
-                                                                     BcBwdPull{dep, lvbm, visited}, ActOut(), ctr);
+      GG_TRY(L.pull(tin, BcBwdPull{dep, lvbm, visited}, ActOut(), ctr));
       GG_TRY(tr.kend());
-      L.launches += 2;
+      L.launches += 1;
     }
     uint32_t pn = (uint32_t)(lev_off[lev] - lev_off[lev - 1]);
     if (pn)

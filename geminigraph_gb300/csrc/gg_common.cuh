@@ -46,13 +46,26 @@ int cuda_status(cudaError_t e, const char *what);
   } while (0)
 
 // ---------------------------------------------------------------- graph
+// Degree bins of one direction, built once at load time (the GB300 form of
+// Graph::tune_chunks, core/graph.hpp:1341-1404): pull kernels give a light
+// list (deg <= LIGHT_DEG) one lane, a medium list one warp, and split every
+// heavy list (deg > HEAVY_DEG) into HEAVY_CHUNK-edge chunks, one block each.
+constexpr uint32_t LIGHT_DEG = 32;
+constexpr uint32_t HEAVY_DEG = 2048;
+constexpr uint32_t HEAVY_CHUNK = 2048;
+
 struct Dir {
   uint64_t *off = nullptr;
   uint32_t *nbr = nullptr;
   float *w = nullptr;
   uint32_t *deg = nullptr;
-  uint32_t *hubs = nullptr;   // vertices with deg > hub_threshold, ascending
-  uint32_t nhubs = 0;
+  uint32_t *med = nullptr;          // LIGHT_DEG < deg <= HEAVY_DEG, ascending
+  uint32_t nmed = 0;
+  uint32_t *heavy = nullptr;        // deg > HEAVY_DEG, ascending
+  uint32_t nheavy = 0;
+  uint32_t *heavy_chunk = nullptr;  // nheavy+1: prefix of per-vertex chunk counts
+  uint32_t *chunk_owner = nullptr;  // nchunks: index into heavy of each chunk
+  uint32_t nchunks = 0;
 };
 
 // Per-call counters written by the activation epilogue of every edge kernel.
@@ -73,7 +86,8 @@ enum WsSlot {
   WS_MSG,                               // per-queue-entry message snapshot (4 or 8 B)
   WS_S0, WS_S1, WS_S2, WS_S3,           // vertex state arrays
   WS_SCAN,                              // scan scratch
-  WS_HUBSUM,                            // per-hub partial results
+  WS_HUBSUM,                            // per-iteration counters (PageRank)
+  WS_PARTIAL,                           // per-chunk partial results of heavy lists
   WS_NSLOTS
 };
 
@@ -98,7 +112,6 @@ struct gg_graph {
   gg::Workspace ws;
   uint64_t graph_bytes = 0;
   int num_sms = 0;
-  uint32_t hub_threshold = 0;
   const void *result[2] = {nullptr, nullptr};
   std::vector<cudaEvent_t> evpool;  // events for per-call kernel timing
 };

@@ -130,15 +130,23 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 }
 
 // ---------------------------------------------------------------- pull
-// Dense mode (core/graph.hpp:1664-1855), reduction form.  One warp owns 32
-// consecutive vertices.  For each vertex with op.want(v): acc = identity,
-// combined over the in-list with op.gather / op.combine -- serially by its
-// own lane when in-degree <= small, else by the whole warp (strided loads,
-// shuffle reduction); then op.finish(v, acc, deg) applies the slot and
-// returns whether v is activated.  Op::Acc is the message type.
+// Dense mode (core/graph.hpp:1664-1855), reduction form.  For each vertex v
+// with op.want(v): acc = op.identity(v) combined (op.combine) with
+// op.gather(d, k) over its in-list, then op.finish(v, acc, deg, tally)
+// applies the slot and returns whether v is activated.  Op::Acc is the
+// message type; op.identity_coop() is the neutral element of combine.
+// Work is split by the direction's degree bins:
+//   pull_light   one warp per 32 consecutive vertices, each lane serially
+//                over a list of <= LIGHT_DEG entries (and every deg-0 vertex);
+//                the warp owns the bitmap word of its 32 vertices
+//   pull_medium  one warp per medium vertex, strided loads + shuffle combine
+//   pull_heavy_partial / pull_heavy_finish
+//                one block per HEAVY_CHUNK-edge chunk of a heavy list, then
+//                one warp per heavy vertex combining its chunks in order
+// The medium and heavy kernels run after pull_light in the same stream and
+// set their bitmap bits atomically.
 template <class Op>
-__global__ void __launch_bounds__(PULL_THREADS)
-    pull_reduce(Dir d, uint32_t V, uint32_t small, Op op, ActOut act, Counters *ctr) {
+__global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op op, ActOut act, Counters *ctr) {
   using Acc = typename Op::Acc;
   Tally t;
   size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
@@ -153,33 +161,101 @@ __global__ void __launch_bounds__(PULL_THREADS)
       e = d.off[v + 1];
     }
     uint32_t deg = (uint32_t)(e - b);
-    Acc acc = op.identity(v);
-    if (todo && deg <= small) {
+    bool a = false;
+    if (todo && deg <= LIGHT_DEG) {
+      Acc acc = op.identity(v);
       for (unsigned long long k = b; k < e; k++) acc = op.combine(acc, op.gather(d, k));
+      a = op.finish(v, acc, deg, t);
     }
-    unsigned coop = __ballot_sync(GG_FULL, todo && deg > small);
-    while (coop) {
-      unsigned leader = __ffs(coop) - 1;
-      coop &= coop - 1;
-      unsigned long long lb = __shfl_sync(GG_FULL, b, leader), le = __shfl_sync(GG_FULL, e, leader);
-      Acc part = op.identity_coop();
-      for (unsigned long long k = lb + lane; k < le; k += 32) part = op.combine(part, op.gather(d, k));
-      part = op.warp_combine(part);
-      if (lane == leader) acc = op.combine(acc, part);
-    }
-    bool a = todo && op.finish(v, acc, deg, t);
     if (act.active_out) pull_activate(a, v, g, act, t);
   }
   t.flush(ctr);
 }
 
-// BFS pull (toolkits/bfs.cpp:60-76): an unvisited vertex takes the FIRST
-// in-neighbour (in CSC order) that is in the active set as its parent.  The
-// cooperative scan keeps that order: the first 32-wide chunk with a hit wins
-// and inside it the lowest lane.
+template <class Op>
+__global__ void __launch_bounds__(PULL_THREADS) pull_medium(Dir d, Op op, ActOut act, Counters *ctr) {
+  using Acc = typename Op::Acc;
+  Tally t;
+  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  unsigned lane = lane_id();
+  for (size_t i = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); i < d.nmed; i += nwarps) {
+    uint32_t v = d.med[i];
+    bool a = false;
+    if (op.want(v)) {
+      unsigned long long b = d.off[v], e = d.off[v + 1];
+      Acc p0 = op.identity_coop(), p1 = op.identity_coop();
+      unsigned long long k = b + lane;
+      for (; k + 32 < e; k += 64) {
+        p0 = op.combine(p0, op.gather(d, k));
+        p1 = op.combine(p1, op.gather(d, k + 32));
+      }
+      if (k < e) p0 = op.combine(p0, op.gather(d, k));
+      Acc part = op.warp_combine(op.combine(p0, p1));
+      if (lane == 0) a = op.finish(v, op.combine(op.identity(v), part), (uint32_t)(e - b), t);
+    }
+    if (act.active_out) push_activate(a, v, act, t);
+  }
+  t.flush(ctr);
+}
+
+template <class Op>
+__global__ void __launch_bounds__(PULL_THREADS)
+    pull_heavy_partial(Dir d, Op op, typename Op::Acc *__restrict__ partials) {
+  using Acc = typename Op::Acc;
+  __shared__ Acc s_part[PULL_THREADS / 32];
+  unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  for (uint32_t c = blockIdx.x; c < d.nchunks; c += gridDim.x) {
+    uint32_t h = d.chunk_owner[c];
+    uint32_t v = d.heavy[h];
+    Acc part = op.identity_coop();
+    if (op.want(v)) {
+      unsigned long long b = d.off[v] + (unsigned long long)(c - d.heavy_chunk[h]) * HEAVY_CHUNK;
+      unsigned long long end = d.off[v + 1];
+      unsigned long long e = b + HEAVY_CHUNK < end ? b + HEAVY_CHUNK : end;
+      for (unsigned long long k = b + threadIdx.x; k < e; k += PULL_THREADS) part = op.combine(part, op.gather(d, k));
+    }
+    part = op.warp_combine(part);
+    if (lane == 0) s_part[w] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      Acc r = s_part[0];
+      for (int i = 1; i < PULL_THREADS / 32; i++) r = op.combine(r, s_part[i]);
+      partials[c] = r;
+    }
+    __syncthreads();
+  }
+}
+
+template <class Op>
+__global__ void __launch_bounds__(PULL_THREADS)
+    pull_heavy_finish(Dir d, Op op, const typename Op::Acc *__restrict__ partials, ActOut act, Counters *ctr) {
+  using Acc = typename Op::Acc;
+  Tally t;
+  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  unsigned lane = lane_id();
+  for (size_t h = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); h < d.nheavy; h += nwarps) {
+    uint32_t v = d.heavy[h];
+    bool a = false;
+    if (op.want(v)) {
+      Acc part = op.identity_coop();
+      for (uint32_t c = d.heavy_chunk[h] + lane; c < d.heavy_chunk[h + 1]; c += 32) part = op.combine(part, partials[c]);
+      part = op.warp_combine(part);
+      if (lane == 0) a = op.finish(v, op.combine(op.identity(v), part), d.deg[v], t);
+    }
+    if (act.active_out) push_activate(a, v, act, t);
+  }
+  t.flush(ctr);
+}
+
+// ---------------------------------------------------------------- BFS pull
+// toolkits/bfs.cpp:60-76: an unvisited vertex takes the FIRST in-neighbour
+// (in CSC order) that is in the active set as its parent.  Every bin keeps
+// that order: lanes scan their own list in order; a warp takes the lowest
+// lane of the first 32-wide chunk with a hit; heavy chunks record the index
+// of their first hit and the finish takes the lowest.
 static __global__ void __launch_bounds__(PULL_THREADS)
-    bfs_pull(Dir d, uint32_t V, uint32_t small, const uint32_t *__restrict__ active_in, uint32_t *parent,
-             ActOut act, Counters *ctr) {
+    bfs_pull_light(Dir d, uint32_t V, const uint32_t *__restrict__ active_in, uint32_t *parent, ActOut act,
+                   Counters *ctr) {
   Tally t;
   size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
   size_t groups = ((size_t)V + 31) / 32;
@@ -193,9 +269,8 @@ static __global__ void __launch_bounds__(PULL_THREADS)
       b = d.off[v];
       e = d.off[v + 1];
     }
-    uint32_t deg = (uint32_t)(e - b);
     uint32_t found = NONE32;
-    if (todo && deg <= small) {
+    if (todo && e - b <= LIGHT_DEG) {
       for (unsigned long long k = b; k < e; k++) {
         uint32_t s = d.nbr[k];
         if (bm_test_ldg(active_in, s)) {
@@ -204,31 +279,91 @@ static __global__ void __launch_bounds__(PULL_THREADS)
         }
       }
     }
-    unsigned coop = __ballot_sync(GG_FULL, todo && deg > small);
-    while (coop) {
-      unsigned leader = __ffs(coop) - 1;
-      coop &= coop - 1;
-      unsigned long long lb = __shfl_sync(GG_FULL, b, leader), le = __shfl_sync(GG_FULL, e, leader);
-      uint32_t fsrc = NONE32;
-      for (unsigned long long base = lb; base < le; base += 32) {
+    bool a = found != NONE32;
+    if (a) parent[v] = found;
+    pull_activate(a, v, g, act, t);
+  }
+  t.flush(ctr);
+}
+
+static __global__ void __launch_bounds__(PULL_THREADS)
+    bfs_pull_medium(Dir d, const uint32_t *__restrict__ active_in, uint32_t *parent, ActOut act, Counters *ctr) {
+  Tally t;
+  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  unsigned lane = lane_id();
+  for (size_t i = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); i < d.nmed; i += nwarps) {
+    uint32_t v = d.med[i];
+    uint32_t found = NONE32;
+    if (!bm_test(act.visited, v)) {
+      unsigned long long b = d.off[v], e = d.off[v + 1];
+      for (unsigned long long base = b; base < e; base += 32) {
         unsigned long long k = base + lane;
         uint32_t s = 0;
         bool hit = false;
-        if (k < le) {
+        if (k < e) {
           s = d.nbr[k];
           hit = bm_test_ldg(active_in, s);
         }
         unsigned m = __ballot_sync(GG_FULL, hit);
         if (m) {
-          fsrc = __shfl_sync(GG_FULL, s, __ffs(m) - 1);
+          found = __shfl_sync(GG_FULL, s, __ffs(m) - 1);
           break;
         }
       }
-      if (lane == leader) found = fsrc;
     }
-    bool a = found != NONE32;
+    bool a = lane == 0 && found != NONE32;
     if (a) parent[v] = found;
-    pull_activate(a, v, g, act, t);
+    push_activate(a, v, act, t);
+  }
+  t.flush(ctr);
+}
+
+// partials[c] = edge index of the chunk's first active in-neighbour, or ~0.
+static __global__ void __launch_bounds__(PULL_THREADS)
+    bfs_heavy_partial(Dir d, const uint32_t *__restrict__ active_in, const uint32_t *__restrict__ visited,
+                      unsigned long long *__restrict__ partials) {
+  __shared__ unsigned long long s_first;
+  for (uint32_t c = blockIdx.x; c < d.nchunks; c += gridDim.x) {
+    uint32_t h = d.chunk_owner[c];
+    uint32_t v = d.heavy[h];
+    if (threadIdx.x == 0) s_first = ~0ull;
+    __syncthreads();
+    if (!bm_test(visited, v)) {
+      unsigned long long b = d.off[v] + (unsigned long long)(c - d.heavy_chunk[h]) * HEAVY_CHUNK;
+      unsigned long long end = d.off[v + 1];
+      unsigned long long e = b + HEAVY_CHUNK < end ? b + HEAVY_CHUNK : end;
+      for (unsigned long long base = b; base < e; base += PULL_THREADS) {
+        unsigned long long k = base + threadIdx.x;
+        bool hit = k < e && bm_test_ldg(active_in, d.nbr[k]);
+        if (hit) atomicMin(&s_first, k);
+        if (__syncthreads_or(hit)) break;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) partials[c] = s_first;
+    __syncthreads();
+  }
+}
+
+static __global__ void __launch_bounds__(PULL_THREADS)
+    bfs_heavy_finish(Dir d, const unsigned long long *__restrict__ partials, uint32_t *parent, ActOut act,
+                     Counters *ctr) {
+  Tally t;
+  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  unsigned lane = lane_id();
+  for (size_t h = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); h < d.nheavy; h += nwarps) {
+    uint32_t v = d.heavy[h];
+    unsigned long long first = ~0ull;
+    if (!bm_test(act.visited, v)) {
+      for (uint32_t c = d.heavy_chunk[h] + lane; c < d.heavy_chunk[h + 1]; c += 32) {
+        unsigned long long p = partials[c];
+        first = p < first ? p : first;
+      }
+      first = warp_min(first);
+    }
+    bool a = lane == 0 && first != ~0ull;
+    if (a) parent[v] = d.nbr[first];
+    push_activate(a, v, act, t);
   }
   t.flush(ctr);
 }
@@ -292,6 +427,53 @@ struct Launch {
     unsigned long long tiles = (total + PUSH_TILE - 1) / PUSH_TILE;
     unsigned long long cap = (unsigned long long)g->num_sms * 8;
     return (unsigned)(tiles < 1 ? 1 : (tiles > cap ? cap : tiles));
+  }
+  unsigned med_grid(const Dir &d) const {
+    return grid_for((size_t)d.nmed * 32, PULL_THREADS, g->num_sms, 8);
+  }
+  unsigned heavy_grid(const Dir &d) const {
+    return grid_for((size_t)d.nchunks * PULL_THREADS, PULL_THREADS, g->num_sms, 8);
+  }
+  unsigned heavy_finish_grid(const Dir &d) const {
+    return grid_for((size_t)d.nheavy * 32, PULL_THREADS, g->num_sms, 8);
+  }
+  // All bins of one dense call, in order: light, medium, heavy chunks, heavy finish.
+  template <class Op>
+  int pull(const Dir &d, const Op &op, const ActOut &act, Counters *ctr) {
+    cudaStream_t s = g->stream;
+    pull_light<Op><<<pull_grid(), PULL_THREADS, 0, s>>>(d, g->V, op, act, ctr);
+    launches += 1;
+    if (d.nmed) {
+      pull_medium<Op><<<med_grid(d), PULL_THREADS, 0, s>>>(d, op, act, ctr);
+      launches += 1;
+    }
+    if (d.nheavy) {
+      typename Op::Acc *part = nullptr;
+      GG_TRY(ws(g, WS_PARTIAL, d.nchunks, &part));
+      pull_heavy_partial<Op><<<heavy_grid(d), PULL_THREADS, 0, s>>>(d, op, part);
+      pull_heavy_finish<Op><<<heavy_finish_grid(d), PULL_THREADS, 0, s>>>(d, op, part, act, ctr);
+      launches += 2;
+    }
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  }
+  int bfs_pull(const Dir &d, const uint32_t *active_in, uint32_t *parent, const ActOut &act, Counters *ctr) {
+    cudaStream_t s = g->stream;
+    bfs_pull_light<<<pull_grid(), PULL_THREADS, 0, s>>>(d, g->V, active_in, parent, act, ctr);
+    launches += 1;
+    if (d.nmed) {
+      bfs_pull_medium<<<med_grid(d), PULL_THREADS, 0, s>>>(d, active_in, parent, act, ctr);
+      launches += 1;
+    }
+    if (d.nheavy) {
+      unsigned long long *part = nullptr;
+      GG_TRY(ws(g, WS_PARTIAL, d.nchunks, &part));
+      bfs_heavy_partial<<<heavy_grid(d), PULL_THREADS, 0, s>>>(d, active_in, act.visited, part);
+      bfs_heavy_finish<<<heavy_finish_grid(d), PULL_THREADS, 0, s>>>(d, part, parent, act, ctr);
+      launches += 2;
+    }
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
   }
   int scan_queue_degrees(const uint32_t *q, uint32_t n, const uint32_t *deg, unsigned long long **P) {
     unsigned long long *p = nullptr, *scratch = nullptr;

@@ -308,14 +308,36 @@ __global__ void degrees_from_offsets(const uint64_t *__restrict__ off, uint32_t 
     deg[v] = (uint32_t)(off[v + 1] - off[v]);
 }
 
-__global__ void collect_hubs(const uint32_t *__restrict__ deg, uint32_t V, uint32_t threshold,
-                             uint32_t *__restrict__ hubs, unsigned *count) {
-  size_t stride = (size_t)gridDim.x * blockDim.x;
-  size_t n = ((size_t)V + 31) / 32 * 32;
-  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-    bool p = v < V && deg[v] > threshold;
-    queue_push(p, (uint32_t)v, hubs, count);
+// 1 if LIGHT/HEAVY bin bounds lo < deg[i] <= hi.
+struct DegInRange {
+  const uint32_t *deg;
+  uint32_t lo, hi;
+  __device__ __forceinline__ uint32_t operator()(size_t i) const {
+    uint32_t d = deg[i];
+    return (d > lo && d <= hi) ? 1u : 0u;
   }
+};
+
+__global__ void compact_by_pos(const uint32_t *__restrict__ deg, uint32_t V, uint32_t lo, uint32_t hi,
+                               const uint32_t *__restrict__ pos, uint32_t *__restrict__ out) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x) {
+    uint32_t d = deg[v];
+    if (d > lo && d <= hi) out[pos[v]] = (uint32_t)v;
+  }
+}
+
+struct HeavyChunkCount {
+  const uint32_t *heavy;
+  const uint32_t *deg;
+  __device__ __forceinline__ uint32_t operator()(size_t i) const {
+    return (deg[heavy[i]] + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
+  }
+};
+
+__global__ void fill_chunk_owner(const uint32_t *__restrict__ heavy_chunk, uint32_t nheavy,
+                                 uint32_t *__restrict__ owner) {
+  for (size_t h = (size_t)blockIdx.x * blockDim.x + threadIdx.x; h < nheavy; h += (size_t)gridDim.x * blockDim.x)
+    for (uint32_t c = heavy_chunk[h]; c < heavy_chunk[h + 1]; c++) owner[c] = (uint32_t)h;
 }
 
 __global__ void gen_rmat_kernel(uint32_t *__restrict__ rec, uint64_t E, uint32_t scale, uint64_t key, int weighted) {
@@ -346,6 +368,54 @@ static int bits_for(uint32_t V) {
   return b;
 }
 
+// Ordered list of the vertices with lo < deg <= hi (scan + scatter).
+static int bin_list(gg_graph *g, const Dir *d, uint32_t lo, uint32_t hi, uint32_t **list, uint32_t *count) {
+  uint32_t V = g->V;
+  uint32_t *pos = nullptr, *scratch = nullptr;
+  GG_CUDA(cudaMalloc(&pos, sizeof(uint32_t) * ((size_t)V + 1)));
+  GG_CUDA(cudaMalloc(&scratch, sizeof(uint32_t) * scan_scratch_elems(V)));
+  GG_CUDA((exclusive_scan<uint32_t, DegInRange>(DegInRange{d->deg, lo, hi}, V, pos, scratch, g->stream, nullptr)));
+  uint32_t n = 0;
+  GG_CUDA(cudaMemcpyAsync(&n, pos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  GG_CUDA(cudaMalloc(list, sizeof(uint32_t) * (n ? n : 1)));
+  if (n) {
+    compact_by_pos<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->deg, V, lo, hi, pos, *list);
+    GG_CUDA(cudaGetLastError());
+  }
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  cudaFree(pos);
+  cudaFree(scratch);
+  *count = n;
+  g->graph_bytes += sizeof(uint32_t) * n;
+  return GG_OK;
+}
+
+// Degree bins of one direction (see Dir).
+static int build_bins(gg_graph *g, Dir *d) {
+  GG_TRY(bin_list(g, d, LIGHT_DEG, HEAVY_DEG, &d->med, &d->nmed));
+  GG_TRY(bin_list(g, d, HEAVY_DEG, 0xffffffffu, &d->heavy, &d->nheavy));
+  GG_CUDA(cudaMalloc(&d->heavy_chunk, sizeof(uint32_t) * ((size_t)d->nheavy + 1)));
+  uint32_t *scratch = nullptr;
+  GG_CUDA(cudaMalloc(&scratch, sizeof(uint32_t) * scan_scratch_elems((size_t)d->nheavy + 1)));
+  GG_CUDA((exclusive_scan<uint32_t, HeavyChunkCount>(HeavyChunkCount{d->heavy, d->deg}, d->nheavy, d->heavy_chunk,
+                                                     scratch, g->stream, nullptr)));
+  uint32_t nc = 0;
+  GG_CUDA(cudaMemcpyAsync(&nc, d->heavy_chunk + d->nheavy, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  cudaFree(scratch);
+  d->nchunks = nc;
+  GG_CUDA(cudaMalloc(&d->chunk_owner, sizeof(uint32_t) * (nc ? nc : 1)));
+  if (d->nheavy) {
+    fill_chunk_owner<<<grid_for(d->nheavy, 128, g->num_sms, 4), 128, 0, g->stream>>>(d->heavy_chunk, d->nheavy,
+                                                                                   d->chunk_owner);
+    GG_CUDA(cudaGetLastError());
+  }
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  g->graph_bytes += sizeof(uint32_t) * ((size_t)d->nheavy + 1 + nc);
+  return GG_OK;
+}
+
 // Builds one direction from keys already written by make_keys.
 static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_alt, uint32_t *v_alt, size_t n,
                      int bits, Dir *d) {
@@ -370,24 +440,7 @@ static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_al
     g->graph_bytes += sizeof(float) * n;
     if (n) GG_CUDA(cudaMemcpyAsync(d->w, vs, sizeof(float) * n, cudaMemcpyDeviceToDevice, g->stream));
   }
-  // hub list: in-lists longer than the pull kernels' warp-cooperative range
-  unsigned *cnt = nullptr;
-  GG_CUDA(cudaMalloc(&cnt, sizeof(unsigned)));
-  GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned), g->stream));
-  uint32_t *tmp = nullptr;
-  GG_CUDA(cudaMalloc(&tmp, sizeof(uint32_t) * ((size_t)V + 1)));
-  collect_hubs<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->deg, V, g->hub_threshold, tmp, cnt);
-  GG_CUDA(cudaGetLastError());
-  unsigned nh = 0;
-  GG_CUDA(cudaMemcpyAsync(&nh, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
-  GG_CUDA(cudaStreamSynchronize(g->stream));
-  d->nhubs = nh;
-  GG_CUDA(cudaMalloc(&d->hubs, sizeof(uint32_t) * (nh ? nh : 1)));
-  if (nh) GG_CUDA(cudaMemcpyAsync(d->hubs, tmp, sizeof(uint32_t) * nh, cudaMemcpyDeviceToDevice, g->stream));
-  GG_CUDA(cudaStreamSynchronize(g->stream));
-  cudaFree(tmp);
-  cudaFree(cnt);
-  g->graph_bytes += sizeof(uint32_t) * nh;
+  GG_TRY(build_bins(g, d));
   return GG_OK;
 }
 
@@ -396,7 +449,10 @@ static void free_dir(Dir *d) {
   if (d->nbr) cudaFree(d->nbr);
   if (d->w) cudaFree(d->w);
   if (d->deg) cudaFree(d->deg);
-  if (d->hubs) cudaFree(d->hubs);
+  if (d->med) cudaFree(d->med);
+  if (d->heavy) cudaFree(d->heavy);
+  if (d->heavy_chunk) cudaFree(d->heavy_chunk);
+  if (d->chunk_owner) cudaFree(d->chunk_owner);
   *d = Dir();
 }
 
@@ -432,7 +488,6 @@ static int graph_create(int device, uint32_t V, int weighted, int symmetric, gg_
   g->V = V;
   g->weighted = weighted ? 1 : 0;
   g->symmetric = symmetric ? 1 : 0;
-  g->hub_threshold = 1u << 14;
   cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);

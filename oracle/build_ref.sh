@@ -50,5 +50,15 @@ for app in bfs cc pagerank sssp bc; do
     -I"$HERE/shim" -I"$SRC" -o "$BIN/$app" "$SRC/toolkits/$app.cpp" -lpthread &
   pids+=($!)
 done
+# drivers: the same toolkits' compute() over several roots on one loaded graph
+for app in bfs cc pagerank sssp bc; do
+  APP=$(echo "$app" | tr a-z A-Z)
+  if [ "$BIN/ref_$app" -nt "$HERE/ref_driver.cpp" ] && [ "$BIN/ref_$app" -nt "$SRC/core/graph.hpp" ]; then
+    continue
+  fi
+  "$CXX" -O3 -std=c++11 -g -fopenmp -march=native -w -DGG_APP_$APP \
+    -I"$HERE/shim" -I"$SRC" -o "$BIN/ref_$app" "$HERE/ref_driver.cpp" -lpthread &
+  pids+=($!)
+done
 for p in "${pids[@]}"; do wait "$p"; done
 echo "build_ref: toolkits in $BIN"

@@ -282,3 +282,52 @@ def test_repeated_runs_are_stable():
     g.bfs(root)
     d2, _ = g.sssp(root)
     assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
+
+
+def test_bfs_dense_parent_is_first_active_in_csc_order():
+    # hub 0 has in-edges from every other vertex (5 heavy chunks); the dense
+    # call must pick the smallest active in-neighbour (bfs.cpp:63-66 with the
+    # CSC sorted by source id), which sits in the third chunk
+    V = 10000
+    s = list(range(1, V - 1)) + [9999] * 1000 + list(range(5000, 6000))
+    d = [0] * (V - 2) + list(range(5000, 6000)) + [0] * 1000
+    s, d = np.array(s, np.uint32), np.array(d, np.uint32)
+    g = gg.Graph.from_edges(V, s, d)
+    parent, st = g.bfs(9999)
+    o = OracleGraph(V, s, d)
+    op, otrace = o.bfs(9999)
+    assert st.rows() == otrace
+    assert otrace[1][0] == 1          # the call that reaches the hub is dense
+    assert parent[0] == op[0] == 5000
+    assert g.info()["adj_entries"] == len(s)
+
+
+def test_pull_bins_cover_all_degrees():
+    # one vertex in each bin, including a heavy list that is not a multiple
+    # of the chunk size, for every reduction toolkit
+    V = 7000
+    s, d = [], []
+    for hub, deg in ((0, 6001), (1, 2049), (2, 2048), (3, 33), (4, 32), (5, 1)):
+        src = np.arange(100, 100 + deg) % V
+        s += src.tolist()
+        d += [hub] * deg
+        s += [hub]
+        d += [int(src[0])]
+    s, d = np.array(s, np.uint32), np.array(d, np.uint32)
+    w = graphgen.weights(8, np.arange(len(s), dtype=np.uint64))
+    g = gg.Graph.from_edges(V, s, d, w)
+    o = OracleGraph(V, s, d, w)
+    r, _, _ = g.pagerank(10)
+    orr, _, _ = o.pagerank(10)
+    assert rel_l1(r, orr) < PR_TOL
+    dist, _ = g.sssp(100)
+    odist, _ = o.sssp(100)
+    assert np.array_equal(dist.view(np.uint32), odist.view(np.uint32))
+    dep, inv, _ = g.bc(100)
+    odep, oinv, _ = o.bc(100)
+    ok = ~np.isnan(odep)
+    assert np.array_equal(np.isnan(dep), np.isnan(odep)) and rel_l1(dep[ok], odep[ok]) < BC_TOL
+    gs = gg.Graph.from_edges(V, s, d, symmetric=True)
+    lab, _ = gs.cc()
+    olab, _ = OracleGraph(V, s, d, symmetric=True).cc()
+    assert np.array_equal(lab, olab)

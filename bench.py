@@ -410,6 +410,8 @@ def gpu_arm(args, dist):
                 "ms_per_step": round(e_max * 1000 / args.steps, 3)},
         "roofline": roofline,
         "gpu_launches": launches,
+        "trace_first_step": [[m, ae, act, round(float(stats[0].call_ms[i]), 4)]
+                             for i, (m, ae, act) in enumerate(stats[0].rows()[:40])] if stats else [],
         "wall_s": round(wall, 3),
         "clocks": clk,
     }

@@ -56,27 +56,30 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
   Counters c;
   GG_TRY(counters_read(g, &c));
   unsigned long long ae = c.edges;
-  uint32_t n = c.qlen;
+  uint32_t n_act = c.activated, nq = c.qlen;
+  bool qvalid = true;  // q[cur] holds the active vertices with out-degree > 0
   int cur = 0;
-  while (n > 0) {
+  while (n_act > 0) {
     bool sparse = ae < g->E / 20;
     tr.add(sparse ? 0 : 1, ae, 0);
     int nx = cur ^ 1;
+    if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[cur], g->out.nz, q[cur], &nq));
     GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
     GG_TRY(counters_reset(g));
     ActOut a;
     a.active_out = bm[nx];
     a.visited = visited;
-    a.q_out = q[nx];
+    a.q_out = sparse ? q[nx] : nullptr;
     a.qlen = &ctr->qlen;
     a.out_deg = g->out.deg;
+    a.queue_nonzero_only = true;
     if (sparse) {
       if (ae > 0) {
         unsigned long long *P;
-        GG_TRY(L.scan_queue_degrees(q[cur], n, g->out.deg, &P));
+        GG_TRY(L.scan_queue_degrees(q[cur], nq, g->out.deg, &P));
         GG_TRY(tr.kbegin());
-        push_lb<BfsPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[cur], P, n, ae, g->out, BfsPush{parent, V}, a,
-                                                                    ctr);
+        push_lb<BfsPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[cur], P, nq, ae, g->out, BfsPush{parent, V},
+                                                                    a, ctr);
         GG_TRY(tr.kend());
         L.launches += 1;
       }
@@ -87,7 +90,9 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
     }
     GG_CUDA(cudaGetLastError());
     GG_TRY(counters_read(g, &c));
-    n = c.qlen;
+    n_act = c.activated;
+    nq = c.qlen;
+    qvalid = sparse;
     ae = c.edges;
     tr.set_activated(c.activated);
     cur = nx;

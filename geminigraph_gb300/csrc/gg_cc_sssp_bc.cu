@@ -99,7 +99,8 @@ struct SsspPull {
 // buffers for pull calls.
 template <typename T, class PushOp, class PullOp>
 static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
-                      uint32_t n, unsigned long long ae, Trace &tr, Launch &L, T **result) {
+                      uint32_t n_act, uint32_t nq, bool qvalid, unsigned long long ae, Trace &tr, Launch &L,
+                      T **result) {
   const uint32_t V = g->V;
   const size_t words = bitmap_words32(V);
   cudaStream_t s = g->stream;
@@ -110,24 +111,26 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
   T *msg;
   GG_TRY(ws(g, WS_MSG, (size_t)V + 1, &msg));
   int c_i = 0;
-  while (n > 0) {
+  while (n_act > 0) {
     bool sparse = ae < g->E / 20;
     tr.add(sparse ? 0 : 1, ae, 0);
     int nx = c_i ^ 1;
+    if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[c_i], g->out.nz, q[c_i], &nq));
     GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
     GG_TRY(counters_reset(g));
     ActOut a;
     a.active_out = bm[nx];
-    a.q_out = q[nx];
+    a.q_out = sparse ? q[nx] : nullptr;
     a.qlen = &ctr->qlen;
     a.out_deg = g->out.deg;
+    a.queue_nonzero_only = true;
     if (sparse) {
       if (ae > 0) {
-        gather_by_queue<T><<<grid_for(n, 256, g->num_sms), 256, 0, s>>>(q[c_i], n, cur, msg);
+        gather_by_queue<T><<<grid_for(nq, 256, g->num_sms), 256, 0, s>>>(q[c_i], nq, cur, msg);
         unsigned long long *P;
-        GG_TRY(L.scan_queue_degrees(q[c_i], n, g->out.deg, &P));
+        GG_TRY(L.scan_queue_degrees(q[c_i], nq, g->out.deg, &P));
         GG_TRY(tr.kbegin());
-        push_lb<PushOp><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[c_i], P, n, ae, g->out, PushOp{cur, msg}, a,
+        push_lb<PushOp><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[c_i], P, nq, ae, g->out, PushOp{cur, msg}, a,
                                                                    ctr);
         GG_TRY(tr.kend());
         L.launches += 2;
@@ -143,7 +146,9 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
     GG_CUDA(cudaGetLastError());
     Counters c;
     GG_TRY(counters_read(g, &c));
-    n = c.qlen;
+    n_act = c.activated;
+    nq = c.qlen;
+    qvalid = sparse;
     ae = c.edges;
     tr.set_activated(c.activated);
     c_i = nx;
@@ -169,13 +174,12 @@ static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   GG_TRY(timed_begin(g));
   // label[v] = v over active_in = all (cc.cpp:31-37)
   iota_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(lab[0], V);
-  iota_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(q[0], V);
   bitmap_fill<<<grid_for(words, 256, g->num_sms), 256, 0, s>>>(bm[0], words, V);
-  L.launches += 3;
+  L.launches += 2;
   GG_CUDA(cudaGetLastError());
   uint32_t *res = nullptr;
-  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, g->nadj, tr, L,
-                                               &res)));
+  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0, false, g->nadj,
+                                               tr, L, &res)));
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
   if (label_host) GG_CUDA(cudaMemcpy(label_host, res, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost));
@@ -225,8 +229,8 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   Counters c;
   GG_TRY(counters_read(g, &c));
   float *res = nullptr;
-  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1, c.edges, tr, L,
-                                                &res)));
+  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1, 1, true, c.edges,
+                                                tr, L, &res)));
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
   if (dist_host) GG_CUDA(cudaMemcpy(dist_host, res, sizeof(float) * V, cudaMemcpyDeviceToHost));
@@ -387,6 +391,7 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
     a.out_deg = g->out.deg;
     a.in_deg = g->in.deg;
     const uint32_t *qin = qlev + lev_off[L_];
+    a.q_out = sparse ? qlev + lev_off.back() : nullptr;
     if (sparse) {
       if (ae > 0) {
         unsigned long long *P;
@@ -405,10 +410,14 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
     GG_CUDA(cudaGetLastError());
     GG_TRY(counters_read(g, &c));
     tr.set_activated(c.activated);
+    n = c.activated;
+    if (!sparse && n > 0) {
+      uint32_t nl = 0;
+      GG_TRY(L.queue_from_bitmap(bm[nx], nullptr, qlev + lev_off.back(), &nl));
+    }
     // visited |= active_out (bc.cpp:91-98)
     bitmap_or<<<grid_for(words, 256, g->num_sms), 256, 0, s>>>(visited, bm[nx], words);
     L.launches += 1;
-    n = c.qlen;
     lev_off.push_back(lev_off.back() + n);
     lev_out.push_back(c.edges);
     lev_in.push_back(c.in_edges);

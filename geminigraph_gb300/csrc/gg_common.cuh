@@ -59,6 +59,7 @@ struct Dir {
   uint32_t *nbr = nullptr;
   float *w = nullptr;
   uint32_t *deg = nullptr;
+  uint32_t *nz = nullptr;           // bitmap: deg > 0
   uint32_t *med = nullptr;          // LIGHT_DEG < deg <= HEAVY_DEG, ascending
   uint32_t nmed = 0;
   uint32_t *heavy = nullptr;        // deg > HEAVY_DEG, ascending
@@ -88,6 +89,8 @@ enum WsSlot {
   WS_SCAN,                              // scan scratch
   WS_HUBSUM,                            // per-iteration counters (PageRank)
   WS_PARTIAL,                           // per-chunk partial results of heavy lists
+  WS_QPOS,                              // per-word queue positions (queue_from_bitmap)
+  WS_SCAN32,                            // scan scratch for 32-bit scans
   WS_NSLOTS
 };
 

@@ -27,17 +27,22 @@ namespace gg {
 
 constexpr uint32_t NONE32 = 0xffffffffu;
 constexpr int PUSH_THREADS = 256;
-constexpr int PUSH_TILE = PUSH_THREADS * 8;
+constexpr int PUSH_TILE = 1024;              // edges per block iteration of push_lb
+constexpr int PUSH_STAGE = PUSH_TILE + 1;    // queue entries a tile spans when each has >= 1 edge
 constexpr int PULL_THREADS = 256;
 
-// Where an edge kernel records activations.
+// Where an edge kernel records activations.  Only push (sparse) calls append
+// to a queue; after a pull (dense) call the next queue, if the next call is
+// sparse, is compacted from the bitmap in vertex order (queue_from_bitmap),
+// which avoids one same-address atomic per warp of activated vertices.
 struct ActOut {
   uint32_t *active_out = nullptr;  // bitmap; null: the call activates nothing
   uint32_t *visited = nullptr;     // also set here when non-null
-  uint32_t *q_out = nullptr;       // next queue
+  uint32_t *q_out = nullptr;       // next queue (push calls); null: none
   unsigned *qlen = nullptr;
   const uint32_t *out_deg = nullptr;
   const uint32_t *in_deg = nullptr;  // optional: also sum in_degree
+  bool queue_nonzero_only = false;   // append only vertices with out_degree > 0
 };
 
 // Push activation: pred may be true for several lanes naming the same
@@ -48,10 +53,11 @@ __device__ __forceinline__ void push_activate(bool pred, uint32_t v, const ActOu
     fresh = bm_set_atomic(a.active_out, v);
     if (fresh && a.visited) atomicOr(a.visited + (v >> 5), 1u << (v & 31));
   }
-  queue_push(fresh, v, a.q_out, a.qlen);
+  uint32_t od = fresh ? a.out_deg[v] : 0u;
+  if (a.q_out) queue_push(fresh && (!a.queue_nonzero_only || od > 0), v, a.q_out, a.qlen);
   if (fresh) {
     t.activated += 1;
-    t.edges += a.out_deg[v];
+    t.edges += od;
     if (a.in_deg) t.in_edges += a.in_deg[v];
   }
 }
@@ -64,7 +70,6 @@ __device__ __forceinline__ void pull_activate(bool act, uint32_t v, size_t g, co
     a.active_out[g] = bits;
     if (a.visited) a.visited[g] |= bits;
   }
-  queue_push(act, v, a.q_out, a.qlen);
   if (act) {
     t.activated += 1;
     t.edges += a.out_deg[v];
@@ -72,8 +77,8 @@ __device__ __forceinline__ void pull_activate(bool act, uint32_t v, size_t g, co
   }
 }
 
-__device__ __forceinline__ uint32_t upper_bound_u64(const unsigned long long *P, uint32_t lo, uint32_t hi,
-                                                    unsigned long long x) {
+template <typename T>
+__device__ __forceinline__ uint32_t upper_bound_idx(const T *P, uint32_t lo, uint32_t hi, T x) {
   // first index in [lo, hi) with P[i] > x (hi if none)
   while (lo < hi) {
     uint32_t mid = lo + ((hi - lo) >> 1);
@@ -89,14 +94,20 @@ __device__ __forceinline__ uint32_t upper_bound_u64(const unsigned long long *P,
 // Sparse mode (core/graph.hpp:1510-1663): for every queued vertex q[i] and
 // every out-edge, op.push(src, i, dst, w) applies the slot and returns
 // whether it may activate dst.  Work is split by EDGES: P is the exclusive
-// prefix of the queued vertices' degrees (P[n] = total), each tile of
-// PUSH_TILE consecutive edges is one block iteration, and each thread finds
-// its edge's vertex by binary search, so a hub's list is spread over as many
-// blocks as it needs and neighbour loads are coalesced.
+// prefix of the queued vertices' degrees (P[n] = total); each block
+// iteration takes PUSH_TILE consecutive edges, stages the tile's slice of P
+// with the sources and their list offsets in shared memory, and each thread
+// finds its edge's source by binary search there.  A hub's list is spread
+// over as many blocks as it needs and neighbour loads are coalesced.  A tile
+// spanning more than PUSH_STAGE entries (queues holding degree-0 vertices)
+// searches P in global memory instead.
 template <class Op>
 __global__ void __launch_bounds__(PUSH_THREADS)
     push_lb(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
             unsigned long long total, Dir d, Op op, ActOut act, Counters *ctr) {
+  __shared__ unsigned long long s_P[PUSH_STAGE + 1];
+  __shared__ unsigned long long s_base[PUSH_STAGE];
+  __shared__ uint32_t s_src[PUSH_STAGE];
   __shared__ uint32_t s_lo, s_hi;
   Tally t;
   unsigned long long ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
@@ -104,27 +115,47 @@ __global__ void __launch_bounds__(PUSH_THREADS)
     unsigned long long e0 = tile * PUSH_TILE;
     unsigned long long e1 = e0 + PUSH_TILE < total ? e0 + PUSH_TILE : total;
     if (threadIdx.x == 0) {
-      s_lo = upper_bound_u64(P, 0, n + 1, e0) - 1;
-      s_hi = upper_bound_u64(P, s_lo, n + 1, e1 - 1);  // one past the entry holding e1-1
+      uint32_t lo = upper_bound_idx<unsigned long long>(P, 0, n + 1, e0) - 1;
+      s_lo = lo;
+      s_hi = upper_bound_idx<unsigned long long>(P, lo, n + 1, e1 - 1);  // one past the entry holding e1-1
     }
     __syncthreads();
-    uint32_t lo = s_lo, hi = s_hi;
+    const uint32_t lo = s_lo, hi = s_hi, cnt = hi - lo;
+    const bool staged = cnt <= (uint32_t)PUSH_STAGE;
+    if (staged) {
+      for (uint32_t i = threadIdx.x; i < cnt; i += PUSH_THREADS) {
+        unsigned long long pi = P[lo + i];
+        uint32_t src = q[lo + i];
+        s_P[i] = pi;
+        s_src[i] = src;
+        s_base[i] = d.off[src] - pi;
+      }
+    }
     __syncthreads();
     for (unsigned long long base = e0; base < e1; base += PUSH_THREADS) {
       unsigned long long e = base + threadIdx.x;
-      bool valid = e < e1;
       bool pred = false;
       uint32_t dst = 0;
-      if (valid) {
-        uint32_t i = upper_bound_u64(P, lo, hi, e) - 1;
-        uint32_t src = q[i];
-        unsigned long long k = d.off[src] + (e - P[i]);
+      if (e < e1) {
+        uint32_t qi, src;
+        unsigned long long k;
+        if (staged) {
+          uint32_t i = upper_bound_idx<unsigned long long>(s_P, 0, cnt, e) - 1;
+          src = s_src[i];
+          k = s_base[i] + e;
+          qi = lo + i;
+        } else {
+          qi = upper_bound_idx<unsigned long long>(P, lo, hi, e) - 1;
+          src = q[qi];
+          k = d.off[src] + (e - P[qi]);
+        }
         dst = d.nbr[k];
         float w = d.w ? d.w[k] : 0.0f;
-        pred = op.push(src, i, dst, w);
+        pred = op.push(src, qi, dst, w);
       }
       if (act.active_out) push_activate(pred, dst, act, t);
     }
+    __syncthreads();
   }
   t.flush(ctr);
 }
@@ -163,8 +194,14 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
     uint32_t deg = (uint32_t)(e - b);
     bool a = false;
     if (todo && deg <= LIGHT_DEG) {
+      // four independent gathers in flight, combined in list order
       Acc acc = op.identity(v);
-      for (unsigned long long k = b; k < e; k++) acc = op.combine(acc, op.gather(d, k));
+      unsigned long long k = b;
+      for (; k + 4 <= e; k += 4) {
+        Acc g0 = op.gather(d, k), g1 = op.gather(d, k + 1), g2 = op.gather(d, k + 2), g3 = op.gather(d, k + 3);
+        acc = op.combine(op.combine(op.combine(op.combine(acc, g0), g1), g2), g3);
+      }
+      for (; k < e; k++) acc = op.combine(acc, op.gather(d, k));
       a = op.finish(v, acc, deg, t);
     }
     if (act.active_out) pull_activate(a, v, g, act, t);
@@ -257,31 +294,73 @@ static __global__ void __launch_bounds__(PULL_THREADS)
     bfs_pull_light(Dir d, uint32_t V, const uint32_t *__restrict__ active_in, uint32_t *parent, ActOut act,
                    Counters *ctr) {
   Tally t;
-  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
-  size_t groups = ((size_t)V + 31) / 32;
-  unsigned lane = lane_id();
-  for (size_t g = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); g < groups; g += nwarps) {
+  const size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  const size_t groups = ((size_t)V + 31) / 32;
+  const unsigned lane = lane_id();
+  // Software-pipelined over the warp's groups: the visited word, offsets and
+  // out-degree of group g + nwarps are loaded before group g is scanned.
+  size_t g = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5);
+  uint32_t vis = 0, od = 0;
+  unsigned long long b = 0, e = 0;
+  bool todo = false;
+  if (g < groups) {
     uint32_t v = (uint32_t)(g * 32 + lane);
-    uint32_t vis = act.visited[g];
-    bool todo = v < V && !((vis >> lane) & 1u);
-    unsigned long long b = 0, e = 0;
+    vis = act.visited[g];
+    todo = v < V && !((vis >> lane) & 1u);
     if (todo) {
       b = d.off[v];
       e = d.off[v + 1];
+      od = act.out_deg[v];
     }
-    uint32_t found = NONE32;
-    if (todo && e - b <= LIGHT_DEG) {
-      for (unsigned long long k = b; k < e; k++) {
-        uint32_t s = d.nbr[k];
-        if (bm_test_ldg(active_in, s)) {
-          found = s;
-          break;
-        }
+  }
+  while (g < groups) {
+    const size_t gn = g + nwarps;
+    uint32_t visn = 0, odn = 0;
+    unsigned long long bn = 0, en = 0;
+    bool todon = false;
+    if (gn < groups) {
+      uint32_t vn = (uint32_t)(gn * 32 + lane);
+      visn = act.visited[gn];
+      todon = vn < V && !((visn >> lane) & 1u);
+      if (todon) {
+        bn = d.off[vn];
+        en = d.off[vn + 1];
+        odn = act.out_deg[vn];
       }
     }
-    bool a = found != NONE32;
+    // the first LIGHT_DEG entries of every list, four independent loads at a
+    // time; longer lists without a hit there go on in the medium / heavy kernels
+    const uint32_t v = (uint32_t)(g * 32 + lane);
+    uint32_t found = NONE32;
+    if (todo) {
+      unsigned long long lim = e - b <= LIGHT_DEG ? e : b + LIGHT_DEG;
+      for (unsigned long long k = b; k < lim && found == NONE32; k += 4) {
+        uint32_t s0 = d.nbr[k];
+        uint32_t s1 = k + 1 < lim ? d.nbr[k + 1] : s0;
+        uint32_t s2 = k + 2 < lim ? d.nbr[k + 2] : s0;
+        uint32_t s3 = k + 3 < lim ? d.nbr[k + 3] : s0;
+        bool h0 = bm_test_ldg(active_in, s0), h1 = bm_test_ldg(active_in, s1);
+        bool h2 = bm_test_ldg(active_in, s2), h3 = bm_test_ldg(active_in, s3);
+        found = h0 ? s0 : h1 ? s1 : h2 ? s2 : h3 ? s3 : NONE32;
+      }
+    }
+    const bool a = found != NONE32;
     if (a) parent[v] = found;
-    pull_activate(a, v, g, act, t);
+    const unsigned bits = __ballot_sync(GG_FULL, a);
+    if (lane == 0 && bits) {
+      act.active_out[g] = bits;
+      act.visited[g] = vis | bits;
+    }
+    if (a) {
+      t.activated += 1;
+      t.edges += od;
+    }
+    g = gn;
+    vis = visn;
+    todo = todon;
+    b = bn;
+    e = en;
+    od = odn;
   }
   t.flush(ctr);
 }
@@ -295,7 +374,7 @@ static __global__ void __launch_bounds__(PULL_THREADS)
     uint32_t v = d.med[i];
     uint32_t found = NONE32;
     if (!bm_test(act.visited, v)) {
-      unsigned long long b = d.off[v], e = d.off[v + 1];
+      unsigned long long b = d.off[v] + LIGHT_DEG, e = d.off[v + 1];
       for (unsigned long long base = b; base < e; base += 32) {
         unsigned long long k = base + lane;
         uint32_t s = 0;
@@ -366,6 +445,33 @@ static __global__ void __launch_bounds__(PULL_THREADS)
     push_activate(a, v, act, t);
   }
   t.flush(ctr);
+}
+
+// ---------------------------------------------------------------- queue from bitmap
+// popcount of (bm & mask) per 32-bit word: the scan input of queue_from_bitmap.
+struct MaskedPopc {
+  const uint32_t *bm;
+  const uint32_t *mask;
+  __device__ __forceinline__ uint32_t operator()(size_t i) const {
+    uint32_t w = bm[i];
+    if (mask) w &= mask[i];
+    return (uint32_t)__popc(w);
+  }
+};
+
+// q[pos[i] ...] = the vertices of word i of (bm & mask), ascending.
+static __global__ void queue_scatter(const uint32_t *__restrict__ bm, const uint32_t *__restrict__ mask,
+                                     size_t words, const uint32_t *__restrict__ pos, uint32_t *__restrict__ q) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t w = bm[i];
+    if (mask) w &= mask[i];
+    uint32_t p = pos[i];
+    while (w) {
+      uint32_t b = __ffs(w) - 1;
+      w &= w - 1;
+      q[p++] = (uint32_t)(i * 32 + b);
+    }
+  }
 }
 
 // ---------------------------------------------------------------- small kernels
@@ -473,6 +579,23 @@ struct Launch {
       launches += 2;
     }
     GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  }
+  // Ordered queue of the set bits of bm (restricted to mask when non-null);
+  // *n receives its length.
+  int queue_from_bitmap(const uint32_t *bm, const uint32_t *mask, uint32_t *q, uint32_t *n) {
+    size_t words = bitmap_words32(g->V);
+    uint32_t *pos = nullptr, *scratch = nullptr;
+    GG_TRY(ws(g, WS_QPOS, words + 1, &pos));
+    GG_TRY(ws(g, WS_SCAN32, scan_scratch_elems(words), &scratch));
+    GG_CUDA((exclusive_scan<uint32_t, MaskedPopc>(MaskedPopc{bm, mask}, words, pos, scratch, g->stream,
+                                                  &launches)));
+    queue_scatter<<<grid_for(words, 256, g->num_sms, 8), 256, 0, g->stream>>>(bm, mask, words, pos, q);
+    launches += 1;
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(g->ws.ctr_host, pos + words, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GG_CUDA(cudaStreamSynchronize(g->stream));
+    *n = *(uint32_t *)g->ws.ctr_host;
     return GG_OK;
   }
   int scan_queue_degrees(const uint32_t *q, uint32_t n, const uint32_t *deg, unsigned long long **P) {

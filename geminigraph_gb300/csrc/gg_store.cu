@@ -303,6 +303,17 @@ __global__ void offsets_from_keys(const uint64_t *__restrict__ keys, size_t n, i
   }
 }
 
+// Bitmap of the vertices with deg > 0 (one warp per 32-bit word).
+__global__ void nonzero_bitmap(const uint32_t *__restrict__ deg, uint32_t V, uint32_t *__restrict__ nz,
+                               size_t words) {
+  size_t nthreads = words * 32;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nthreads; i += (size_t)gridDim.x * blockDim.x) {
+    bool p = i < V && deg[i] > 0;
+    unsigned b = __ballot_sync(GG_FULL, p);
+    if ((threadIdx.x & 31) == 0) nz[i >> 5] = b;
+  }
+}
+
 __global__ void degrees_from_offsets(const uint64_t *__restrict__ off, uint32_t V, uint32_t *__restrict__ deg) {
   for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
     deg[v] = (uint32_t)(off[v + 1] - off[v]);
@@ -440,6 +451,11 @@ static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_al
     g->graph_bytes += sizeof(float) * n;
     if (n) GG_CUDA(cudaMemcpyAsync(d->w, vs, sizeof(float) * n, cudaMemcpyDeviceToDevice, g->stream));
   }
+  size_t words = bitmap_words32(V);
+  GG_CUDA(cudaMalloc(&d->nz, sizeof(uint32_t) * words));
+  g->graph_bytes += sizeof(uint32_t) * words;
+  nonzero_bitmap<<<grid_for(words * 32, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->deg, V, d->nz, words);
+  GG_CUDA(cudaGetLastError());
   GG_TRY(build_bins(g, d));
   return GG_OK;
 }
@@ -449,6 +465,7 @@ static void free_dir(Dir *d) {
   if (d->nbr) cudaFree(d->nbr);
   if (d->w) cudaFree(d->w);
   if (d->deg) cudaFree(d->deg);
+  if (d->nz) cudaFree(d->nz);
   if (d->med) cudaFree(d->med);
   if (d->heavy) cudaFree(d->heavy);
   if (d->heavy_chunk) cudaFree(d->heavy_chunk);

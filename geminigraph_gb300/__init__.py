@@ -77,6 +77,7 @@ def library():
         "gg_result_device_ptr": ([vp, i32], vp),
         "gg_active_edges": ([vp, vp, ctypes.POINTER(u64)], i32),
         "gg_is_sparse": ([u64, u64], i32),
+        "gg_active_edges_noalloc": ([vp, vp, u32, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

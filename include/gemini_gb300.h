@@ -153,6 +153,24 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
  * vertices/64 + 1 of them). */
 int gg_active_edges(gg_graph *g, const uint64_t *active_bitmap, uint64_t *active_edges);
 
+/* No counterpart in the reference.  gg_active_edges for callers that cannot
+ * let a library allocate device memory: a serving process that reserves all of
+ * HBM for its own pool at start-up, or a latency-critical caller that cannot
+ * take the device synchronisation of cudaMalloc/cudaFree.  All pointers are
+ * device memory the caller provides: d_bitmap (vertices/64+1 64-bit words, the
+ * reference's bitmap layout), d_degree (vertices out-degrees), d_active_edges
+ * (one uint64 that receives the sum).  stream is a cudaStream_t, or NULL for
+ * the default stream; the call returns once that stream has finished.
+ * It allocates nothing: its only scratch is a fixed 32 KiB device array inside
+ * the library (one partial sum per 65,536 vertices), so it accepts at most
+ * GG_NOALLOC_MAX_VERTICES vertices and returns GG_ERR_LIMIT beyond.  The first
+ * call on a device looks up that array's device address (cudaGetSymbolAddress):
+ * make that first call before any stream capture.  All calls share the array,
+ * which keeps the last call's partial sums; calls that overlap on the GPU race. */
+#define GG_NOALLOC_MAX_VERTICES 268435456u
+int gg_active_edges_noalloc(const uint64_t *d_bitmap, const uint32_t *d_degree, uint32_t vertices,
+                            uint64_t *d_active_edges, void *stream);
+
 /* The sparse/dense switch of process_edges (core/graph.hpp:1509). */
 int gg_is_sparse(uint64_t active_edges, uint64_t edges);
 

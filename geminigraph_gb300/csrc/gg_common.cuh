@@ -53,6 +53,7 @@ int cuda_status(cudaError_t e, const char *what);
 constexpr uint32_t LIGHT_DEG = 32;
 constexpr uint32_t HEAVY_DEG = 2048;
 constexpr uint32_t HEAVY_CHUNK = 2048;
+constexpr uint32_t PULL_CHUNK = 256;   // reduction pulls: edges per warp work item
 
 struct Dir {
   uint64_t *off = nullptr;
@@ -67,6 +68,11 @@ struct Dir {
   uint32_t *heavy_chunk = nullptr;  // nheavy+1: prefix of per-vertex chunk counts
   uint32_t *chunk_owner = nullptr;  // nchunks: index into heavy of each chunk
   uint32_t nchunks = 0;
+  uint32_t *big = nullptr;          // deg > LIGHT_DEG, ascending (reduction pulls)
+  uint32_t nbig = 0;
+  uint32_t *big_chunk = nullptr;    // nbig+1: prefix of per-vertex PULL_CHUNK counts
+  uint32_t *big_owner = nullptr;    // nbigchunks: index into big of each chunk
+  uint32_t nbigchunks = 0;
 };
 
 // Per-call counters written by the activation epilogue of every edge kernel.

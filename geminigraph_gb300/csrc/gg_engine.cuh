@@ -170,12 +170,12 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 //   pull_light   one warp per 32 consecutive vertices, each lane serially
 //                over a list of <= LIGHT_DEG entries (and every deg-0 vertex);
 //                the warp owns the bitmap word of its 32 vertices
-//   pull_medium  one warp per medium vertex, strided loads + shuffle combine
-//   pull_heavy_partial / pull_heavy_finish
-//                one block per HEAVY_CHUNK-edge chunk of a heavy list, then
-//                one warp per heavy vertex combining its chunks in order
-// The medium and heavy kernels run after pull_light in the same stream and
-// set their bitmap bits atomically.
+//   pull_chunks / pull_big_finish
+//                every longer list cut into PULL_CHUNK-edge chunks, one warp
+//                per chunk, then one lane per vertex combining its chunks in
+//                order
+// The chunk kernels run after pull_light in the same stream and set their
+// bitmap bits atomically.
 template <class Op>
 __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op op, ActOut act, Counters *ctr) {
   using Acc = typename Op::Acc;
@@ -209,76 +209,70 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
   t.flush(ctr);
 }
 
-template <class Op>
-__global__ void __launch_bounds__(PULL_THREADS) pull_medium(Dir d, Op op, ActOut act, Counters *ctr) {
-  using Acc = typename Op::Acc;
-  Tally t;
-  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
-  unsigned lane = lane_id();
-  for (size_t i = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); i < d.nmed; i += nwarps) {
-    uint32_t v = d.med[i];
-    bool a = false;
-    if (op.want(v)) {
-      unsigned long long b = d.off[v], e = d.off[v + 1];
-      Acc p0 = op.identity_coop(), p1 = op.identity_coop();
-      unsigned long long k = b + lane;
-      for (; k + 32 < e; k += 64) {
-        p0 = op.combine(p0, op.gather(d, k));
-        p1 = op.combine(p1, op.gather(d, k + 32));
-      }
-      if (k < e) p0 = op.combine(p0, op.gather(d, k));
-      Acc part = op.warp_combine(op.combine(p0, p1));
-      if (lane == 0) a = op.finish(v, op.combine(op.identity(v), part), (uint32_t)(e - b), t);
-    }
-    if (act.active_out) push_activate(a, v, act, t);
-  }
-  t.flush(ctr);
-}
-
+// Lists longer than LIGHT_DEG: one warp per PULL_CHUNK-edge chunk, eight
+// independent gathers in flight per lane; partials[c] = the chunk's combine.
 template <class Op>
 __global__ void __launch_bounds__(PULL_THREADS)
-    pull_heavy_partial(Dir d, Op op, typename Op::Acc *__restrict__ partials) {
+    pull_chunks(Dir d, Op op, typename Op::Acc *__restrict__ partials) {
   using Acc = typename Op::Acc;
-  __shared__ Acc s_part[PULL_THREADS / 32];
-  unsigned lane = lane_id(), w = threadIdx.x >> 5;
-  for (uint32_t c = blockIdx.x; c < d.nchunks; c += gridDim.x) {
-    uint32_t h = d.chunk_owner[c];
-    uint32_t v = d.heavy[h];
+  constexpr int PER_LANE = PULL_CHUNK / 32;
+  const size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  const unsigned lane = lane_id();
+  for (size_t c = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); c < d.nbigchunks; c += nwarps) {
+    const uint32_t o = d.big_owner[c];
+    const uint32_t v = d.big[o];
     Acc part = op.identity_coop();
     if (op.want(v)) {
-      unsigned long long b = d.off[v] + (unsigned long long)(c - d.heavy_chunk[h]) * HEAVY_CHUNK;
-      unsigned long long end = d.off[v + 1];
-      unsigned long long e = b + HEAVY_CHUNK < end ? b + HEAVY_CHUNK : end;
-      for (unsigned long long k = b + threadIdx.x; k < e; k += PULL_THREADS) part = op.combine(part, op.gather(d, k));
+      const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * PULL_CHUNK;
+      const unsigned long long end = d.off[v + 1];
+      const unsigned long long e = b + PULL_CHUNK < end ? b + PULL_CHUNK : end;
+      Acc vals[PER_LANE];
+#pragma unroll
+      for (int j = 0; j < PER_LANE; j++) {
+        unsigned long long k = b + lane + 32 * j;
+        vals[j] = k < e ? op.gather(d, k) : op.identity_coop();
+      }
+#pragma unroll
+      for (int j = 0; j < PER_LANE; j++) part = op.combine(part, vals[j]);
     }
     part = op.warp_combine(part);
-    if (lane == 0) s_part[w] = part;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      Acc r = s_part[0];
-      for (int i = 1; i < PULL_THREADS / 32; i++) r = op.combine(r, s_part[i]);
-      partials[c] = r;
-    }
-    __syncthreads();
+    if (lane == 0) partials[c] = part;
   }
 }
 
+// One lane per long-list vertex combines its chunk partials in order (a warp
+// does it for vertices with more than 32 chunks), then applies the slot.
 template <class Op>
 __global__ void __launch_bounds__(PULL_THREADS)
-    pull_heavy_finish(Dir d, Op op, const typename Op::Acc *__restrict__ partials, ActOut act, Counters *ctr) {
+    pull_big_finish(Dir d, Op op, const typename Op::Acc *__restrict__ partials, ActOut act, Counters *ctr) {
   using Acc = typename Op::Acc;
   Tally t;
-  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
-  unsigned lane = lane_id();
-  for (size_t h = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); h < d.nheavy; h += nwarps) {
-    uint32_t v = d.heavy[h];
-    bool a = false;
-    if (op.want(v)) {
-      Acc part = op.identity_coop();
-      for (uint32_t c = d.heavy_chunk[h] + lane; c < d.heavy_chunk[h + 1]; c += 32) part = op.combine(part, partials[c]);
-      part = op.warp_combine(part);
-      if (lane == 0) a = op.finish(v, op.combine(op.identity(v), part), d.deg[v], t);
+  const size_t stride = (size_t)gridDim.x * PULL_THREADS;
+  const size_t n = ((size_t)d.nbig + 31) / 32 * 32;
+  const unsigned lane = lane_id();
+  for (size_t i = (size_t)blockIdx.x * PULL_THREADS + threadIdx.x; i < n; i += stride) {
+    const bool valid = i < d.nbig;
+    const uint32_t v = valid ? d.big[i] : 0u;
+    const bool todo = valid && op.want(v);
+    uint32_t c0 = 0, c1 = 0;
+    if (todo) {
+      c0 = d.big_chunk[i];
+      c1 = d.big_chunk[i + 1];
     }
+    Acc acc = op.identity(v);
+    if (todo && c1 - c0 <= 32)
+      for (uint32_t c = c0; c < c1; c++) acc = op.combine(acc, partials[c]);
+    unsigned coop = __ballot_sync(GG_FULL, todo && c1 - c0 > 32);
+    while (coop) {
+      const unsigned leader = __ffs(coop) - 1;
+      coop &= coop - 1;
+      const uint32_t lc0 = __shfl_sync(GG_FULL, c0, leader), lc1 = __shfl_sync(GG_FULL, c1, leader);
+      Acc part = op.identity_coop();
+      for (uint32_t c = lc0 + lane; c < lc1; c += 32) part = op.combine(part, partials[c]);
+      part = op.warp_combine(part);
+      if (lane == leader) acc = op.combine(acc, part);
+    }
+    const bool a = todo && op.finish(v, acc, d.deg[v], t);
     if (act.active_out) push_activate(a, v, act, t);
   }
   t.flush(ctr);
@@ -290,7 +284,7 @@ __global__ void __launch_bounds__(PULL_THREADS)
 // that order: lanes scan their own list in order; a warp takes the lowest
 // lane of the first 32-wide chunk with a hit; heavy chunks record the index
 // of their first hit and the finish takes the lowest.
-static __global__ void __launch_bounds__(PULL_THREADS)
+static __global__ void __launch_bounds__(PULL_THREADS, 8)
     bfs_pull_light(Dir d, uint32_t V, const uint32_t *__restrict__ active_in, uint32_t *parent, ActOut act,
                    Counters *ctr) {
   Tally t;
@@ -549,15 +543,13 @@ struct Launch {
     cudaStream_t s = g->stream;
     pull_light<Op><<<pull_grid(), PULL_THREADS, 0, s>>>(d, g->V, op, act, ctr);
     launches += 1;
-    if (d.nmed) {
-      pull_medium<Op><<<med_grid(d), PULL_THREADS, 0, s>>>(d, op, act, ctr);
-      launches += 1;
-    }
-    if (d.nheavy) {
+    if (d.nbig) {
       typename Op::Acc *part = nullptr;
-      GG_TRY(ws(g, WS_PARTIAL, d.nchunks, &part));
-      pull_heavy_partial<Op><<<heavy_grid(d), PULL_THREADS, 0, s>>>(d, op, part);
-      pull_heavy_finish<Op><<<heavy_finish_grid(d), PULL_THREADS, 0, s>>>(d, op, part, act, ctr);
+      GG_TRY(ws(g, WS_PARTIAL, d.nbigchunks, &part));
+      pull_chunks<Op><<<grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(
+          d, op, part);
+      pull_big_finish<Op><<<grid_for(d.nbig, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, op, part, act,
+                                                                                                  ctr);
       launches += 2;
     }
     GG_CUDA(cudaGetLastError());

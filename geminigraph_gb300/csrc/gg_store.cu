@@ -337,12 +337,11 @@ __global__ void compact_by_pos(const uint32_t *__restrict__ deg, uint32_t V, uin
   }
 }
 
-struct HeavyChunkCount {
-  const uint32_t *heavy;
+struct ChunkCount {
+  const uint32_t *list;
   const uint32_t *deg;
-  __device__ __forceinline__ uint32_t operator()(size_t i) const {
-    return (deg[heavy[i]] + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
-  }
+  uint32_t chunk;
+  __device__ __forceinline__ uint32_t operator()(size_t i) const { return (deg[list[i]] + chunk - 1) / chunk; }
 };
 
 __global__ void fill_chunk_owner(const uint32_t *__restrict__ heavy_chunk, uint32_t nheavy,
@@ -402,28 +401,37 @@ static int bin_list(gg_graph *g, const Dir *d, uint32_t lo, uint32_t hi, uint32_
   return GG_OK;
 }
 
+// Chunk table of a vertex list: *prefix (n+1) of ceil(deg/chunk), *owner[c] =
+// list index of chunk c.
+static int chunk_table(gg_graph *g, const Dir *d, const uint32_t *list, uint32_t n, uint32_t chunk,
+                       uint32_t **prefix, uint32_t **owner, uint32_t *nchunks) {
+  GG_CUDA(cudaMalloc(prefix, sizeof(uint32_t) * ((size_t)n + 1)));
+  uint32_t *scratch = nullptr;
+  GG_CUDA(cudaMalloc(&scratch, sizeof(uint32_t) * scan_scratch_elems((size_t)n + 1)));
+  GG_CUDA((exclusive_scan<uint32_t, ChunkCount>(ChunkCount{list, d->deg, chunk}, n, *prefix, scratch, g->stream,
+                                                nullptr)));
+  uint32_t nc = 0;
+  GG_CUDA(cudaMemcpyAsync(&nc, *prefix + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  cudaFree(scratch);
+  *nchunks = nc;
+  GG_CUDA(cudaMalloc(owner, sizeof(uint32_t) * (nc ? nc : 1)));
+  if (n) {
+    fill_chunk_owner<<<grid_for(n, 128, g->num_sms, 8), 128, 0, g->stream>>>(*prefix, n, *owner);
+    GG_CUDA(cudaGetLastError());
+  }
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  g->graph_bytes += sizeof(uint32_t) * ((size_t)n + 1 + nc);
+  return GG_OK;
+}
+
 // Degree bins of one direction (see Dir).
 static int build_bins(gg_graph *g, Dir *d) {
   GG_TRY(bin_list(g, d, LIGHT_DEG, HEAVY_DEG, &d->med, &d->nmed));
   GG_TRY(bin_list(g, d, HEAVY_DEG, 0xffffffffu, &d->heavy, &d->nheavy));
-  GG_CUDA(cudaMalloc(&d->heavy_chunk, sizeof(uint32_t) * ((size_t)d->nheavy + 1)));
-  uint32_t *scratch = nullptr;
-  GG_CUDA(cudaMalloc(&scratch, sizeof(uint32_t) * scan_scratch_elems((size_t)d->nheavy + 1)));
-  GG_CUDA((exclusive_scan<uint32_t, HeavyChunkCount>(HeavyChunkCount{d->heavy, d->deg}, d->nheavy, d->heavy_chunk,
-                                                     scratch, g->stream, nullptr)));
-  uint32_t nc = 0;
-  GG_CUDA(cudaMemcpyAsync(&nc, d->heavy_chunk + d->nheavy, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
-  GG_CUDA(cudaStreamSynchronize(g->stream));
-  cudaFree(scratch);
-  d->nchunks = nc;
-  GG_CUDA(cudaMalloc(&d->chunk_owner, sizeof(uint32_t) * (nc ? nc : 1)));
-  if (d->nheavy) {
-    fill_chunk_owner<<<grid_for(d->nheavy, 128, g->num_sms, 4), 128, 0, g->stream>>>(d->heavy_chunk, d->nheavy,
-                                                                                   d->chunk_owner);
-    GG_CUDA(cudaGetLastError());
-  }
-  GG_CUDA(cudaStreamSynchronize(g->stream));
-  g->graph_bytes += sizeof(uint32_t) * ((size_t)d->nheavy + 1 + nc);
+  GG_TRY(chunk_table(g, d, d->heavy, d->nheavy, HEAVY_CHUNK, &d->heavy_chunk, &d->chunk_owner, &d->nchunks));
+  GG_TRY(bin_list(g, d, LIGHT_DEG, 0xffffffffu, &d->big, &d->nbig));
+  GG_TRY(chunk_table(g, d, d->big, d->nbig, PULL_CHUNK, &d->big_chunk, &d->big_owner, &d->nbigchunks));
   return GG_OK;
 }
 
@@ -470,6 +478,9 @@ static void free_dir(Dir *d) {
   if (d->heavy) cudaFree(d->heavy);
   if (d->heavy_chunk) cudaFree(d->heavy_chunk);
   if (d->chunk_owner) cudaFree(d->chunk_owner);
+  if (d->big) cudaFree(d->big);
+  if (d->big_chunk) cudaFree(d->big_chunk);
+  if (d->big_owner) cudaFree(d->big_owner);
   *d = Dir();
 }
 

@@ -22,6 +22,7 @@ __global__ void bfs_root(uint32_t *parent, uint32_t root, uint32_t *visited, uin
   active[root >> 5] |= 1u << (root & 31);
   q[0] = root;
   ctr->edges = out_deg[root];
+  ctr->maxdeg = out_deg[root];
   ctr->activated = 1;
   ctr->qlen = 1;
 }
@@ -56,11 +57,22 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
   Counters c;
   GG_TRY(counters_read(g, &c));
   unsigned long long ae = c.edges;
-  uint32_t n_act = c.activated, nq = c.qlen;
+  uint32_t n_act = c.activated, nq = c.qlen, md = c.maxdeg;
   bool qvalid = true;  // q[cur] holds the active vertices with out-degree > 0
   int cur = 0;
   while (n_act > 0) {
     bool sparse = ae < g->E / 20;
+    if (sparse && qvalid && Launch::small_ok(nq, ae, md)) {
+      // consecutive small sparse calls run on the device without host round trips
+      GG_TRY((L.small_run<BfsPush, true, uint32_t>(g->out, BfsPush{parent, V}, q, &cur, &nq, &ae, &md, &n_act, visited,
+                                                   nullptr, nullptr, nullptr, tr, nullptr)));
+      if (n_act > 0) {  // the next call is dense or large: its active set is q[cur]
+        GG_CUDA(cudaMemsetAsync(bm[cur], 0, words * 4, s));
+        if (nq) bitmap_from_queue<<<grid_for(nq, 256, g->num_sms), 256, 0, s>>>(q[cur], nq, bm[cur]);
+        L.launches += 1;
+      }
+      continue;
+    }
     tr.add(sparse ? 0 : 1, ae, 0);
     int nx = cur ^ 1;
     if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[cur], g->out.nz, q[cur], &nq));
@@ -92,6 +104,7 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
     GG_TRY(counters_read(g, &c));
     n_act = c.activated;
     nq = c.qlen;
+    md = c.maxdeg;
     qvalid = sparse;
     ae = c.edges;
     tr.set_activated(c.activated);

@@ -99,8 +99,8 @@ struct SsspPull {
 // buffers for pull calls.
 template <typename T, class PushOp, class PullOp>
 static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
-                      uint32_t n_act, uint32_t nq, bool qvalid, unsigned long long ae, Trace &tr, Launch &L,
-                      T **result) {
+                      uint32_t n_act, uint32_t nq, uint32_t md, bool qvalid, unsigned long long ae, Trace &tr,
+                      Launch &L, T **result) {
   const uint32_t V = g->V;
   const size_t words = bitmap_words32(V);
   cudaStream_t s = g->stream;
@@ -109,10 +109,19 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
   uint32_t *q[2] = {q0, q1};
   uint32_t *bm[2] = {bm0, bm1};
   T *msg;
+  uint32_t *stamp;
   GG_TRY(ws(g, WS_MSG, (size_t)V + 1, &msg));
+  GG_TRY(ws(g, WS_STAMP, V, &stamp));
+  GG_CUDA(cudaMemsetAsync(stamp, 0, sizeof(uint32_t) * V, s));
   int c_i = 0;
   while (n_act > 0) {
     bool sparse = ae < g->E / 20;
+    if (sparse && qvalid && Launch::small_ok(nq, ae, md)) {
+      // consecutive small sparse calls run on the device without host round trips
+      GG_TRY((L.small_run<PushOp, false, T>(g->out, PushOp{cur, msg}, q, &c_i, &nq, &ae, &md, &n_act, nullptr, nullptr,
+                                            cur, msg, tr, stamp)));
+      continue;
+    }
     tr.add(sparse ? 0 : 1, ae, 0);
     int nx = c_i ^ 1;
     if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[c_i], g->out.nz, q[c_i], &nq));
@@ -148,6 +157,7 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
     GG_TRY(counters_read(g, &c));
     n_act = c.activated;
     nq = c.qlen;
+    md = c.maxdeg;
     qvalid = sparse;
     ae = c.edges;
     tr.set_activated(c.activated);
@@ -178,7 +188,7 @@ static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   L.launches += 2;
   GG_CUDA(cudaGetLastError());
   uint32_t *res = nullptr;
-  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0, false, g->nadj,
+  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0, 0xffffffffu, false, g->nadj,
                                                tr, L, &res)));
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
@@ -194,6 +204,7 @@ __global__ void sssp_root(float *dist, uint32_t root, uint32_t *active, uint32_t
   active[root >> 5] |= 1u << (root & 31);
   q[0] = root;
   ctr->edges = out_deg[root];
+  ctr->maxdeg = out_deg[root];
 }
 
 static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *st) {
@@ -229,7 +240,7 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   Counters c;
   GG_TRY(counters_read(g, &c));
   float *res = nullptr;
-  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1, 1, true, c.edges,
+  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1, 1, c.maxdeg, true, c.edges,
                                                 tr, L, &res)));
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());

@@ -83,7 +83,7 @@ struct Counters {
   unsigned int qlen;            // entries appended to the output queue
   double delta;                 // PageRank delta accumulator
   unsigned int err;             // device-side error flag (bounds checks)
-  unsigned int pad;
+  unsigned int maxdeg;          // largest out_degree among newly activated vertices
 };
 
 enum WsSlot {
@@ -96,6 +96,8 @@ enum WsSlot {
   WS_HUBSUM,                            // per-iteration counters (PageRank)
   WS_PARTIAL,                           // per-chunk partial results of heavy lists
   WS_QPOS,                              // per-word queue positions (queue_from_bitmap)
+  WS_STAMP,                             // per-vertex activation stamps (small sparse runs)
+  WS_SMALL,                             // SmallRun state and its trace rows
   WS_SCAN32,                            // scan scratch for 32-bit scans
   WS_NSLOTS
 };
@@ -241,20 +243,23 @@ __device__ __forceinline__ void queue_push(bool pred, uint32_t v, uint32_t *q, u
 struct Tally {
   unsigned long long edges = 0, in_edges = 0;
   unsigned int activated = 0;
+  unsigned int maxdeg = 0;
   double delta = 0.0;
   // all threads of the block must call flush
   __device__ __forceinline__ void flush(Counters *ctr) {
     __shared__ unsigned long long s_e[32], s_i[32];
-    __shared__ unsigned int s_a[32];
+    __shared__ unsigned int s_a[32], s_m[32];
     __shared__ double s_d[32];
     unsigned long long e = warp_sum(edges), ie = warp_sum(in_edges);
     unsigned int a = warp_sum(activated);
+    unsigned int m = __reduce_max_sync(GG_FULL, maxdeg);
     double dl = warp_sum(delta);
     unsigned w = threadIdx.x >> 5, lane = lane_id();
     if (lane == 0) {
       s_e[w] = e;
       s_i[w] = ie;
       s_a[w] = a;
+      s_m[w] = m;
       s_d[w] = dl;
     }
     __syncthreads();
@@ -263,12 +268,15 @@ struct Tally {
       e = lane < nw ? s_e[lane] : 0ull;
       ie = lane < nw ? s_i[lane] : 0ull;
       a = lane < nw ? s_a[lane] : 0u;
+      m = lane < nw ? s_m[lane] : 0u;
       dl = lane < nw ? s_d[lane] : 0.0;
       e = warp_sum(e);
       ie = warp_sum(ie);
       a = warp_sum(a);
+      m = __reduce_max_sync(GG_FULL, m);
       dl = warp_sum(dl);
       if (lane == 0) {
+        if (m) atomicMax(&ctr->maxdeg, m);
         if (e) atomicAdd(&ctr->edges, e);
         if (ie) atomicAdd(&ctr->in_edges, ie);
         if (a) atomicAdd(&ctr->activated, a);

@@ -20,6 +20,8 @@
 #ifndef GG_ENGINE_CUH
 #define GG_ENGINE_CUH
 
+#include <string.h>
+
 #include "gg_common.cuh"
 #include "gg_scan.cuh"
 
@@ -58,6 +60,7 @@ __device__ __forceinline__ void push_activate(bool pred, uint32_t v, const ActOu
   if (fresh) {
     t.activated += 1;
     t.edges += od;
+    t.maxdeg = od > t.maxdeg ? od : t.maxdeg;
     if (a.in_deg) t.in_edges += a.in_deg[v];
   }
 }
@@ -71,8 +74,10 @@ __device__ __forceinline__ void pull_activate(bool act, uint32_t v, size_t g, co
     if (a.visited) a.visited[g] |= bits;
   }
   if (act) {
+    const uint32_t od = a.out_deg[v];
     t.activated += 1;
-    t.edges += a.out_deg[v];
+    t.edges += od;
+    t.maxdeg = od > t.maxdeg ? od : t.maxdeg;
     if (a.in_deg) t.in_edges += a.in_deg[v];
   }
 }
@@ -348,6 +353,7 @@ static __global__ void __launch_bounds__(PULL_THREADS, 8)
     if (a) {
       t.activated += 1;
       t.edges += od;
+      t.maxdeg = od > t.maxdeg ? od : t.maxdeg;
     }
     g = gn;
     vis = visn;
@@ -439,6 +445,147 @@ static __global__ void __launch_bounds__(PULL_THREADS)
     push_activate(a, v, act, t);
   }
   t.flush(ctr);
+}
+
+// ---------------------------------------------------------------- small sparse runs
+// A run of consecutive sparse calls whose frontiers are small (high-diameter
+// graphs such as grids, and the tails of power-law BFS) is driven from the
+// device: each call is one push_small launch (plus a snapshot gather for CC
+// and SSSP) that reads its queue length and active_edges from SmallRun; the
+// last block to finish (a ticket counter, no waiting) writes the call's trace
+// row, moves the accumulated counters to the next call, and decides whether
+// the next call may also run here -- the same switch (sparse iff active_edges
+// < edges/20) plus size limits.  The host enqueues a batch of launches without
+// synchronising; launches after the run stops return at once.
+constexpr int SMALL_THREADS = 256;
+constexpr uint32_t SMALL_BATCH = 512;        // calls enqueued per host round trip
+constexpr uint32_t SMALL_MAX_QUEUE = 65536;  // largest queue a small call takes
+constexpr unsigned long long SMALL_MAX_AE = 1ull << 20;
+constexpr uint32_t SMALL_MAX_DEG = 1024;     // largest out-degree in a small call's queue
+
+struct SmallRun {
+  unsigned long long ae;         // active_edges of the call about to run
+  unsigned long long edges_lim;  // edges / 20
+  unsigned long long total_ae;   // sum of active_edges over the run's calls
+  unsigned int n;                // its queue length
+  unsigned int go;               // the next launch runs a call
+  unsigned int calls;            // trace rows written in this batch
+  unsigned int level;            // activation stamp of the current call (> 0)
+  unsigned int ticket;           // blocks finished in the current call
+  unsigned int last_activated;   // activated count of the last call
+  unsigned int maxdeg;           // largest out-degree in the queue of the call about to run
+  Counters next;                 // accumulators of the current call
+};
+
+// Activation inside a small push call: stamp-deduplicated unless the op's
+// slot already lets one thread win (BFS's CAS).  Lanes may be divergent.
+template <bool kUnique>
+__device__ __forceinline__ void small_activate(uint32_t v, SmallRun *st, uint32_t *stamp, unsigned level,
+                                               uint32_t *visited, uint32_t *q_out, const uint32_t *out_deg,
+                                               const uint32_t *in_deg, Tally &t) {
+  if (!kUnique) {
+    if (stamp[v] == level || atomicExch(stamp + v, level) == level) return;
+  }
+  if (visited) atomicOr(visited + (v >> 5), 1u << (v & 31));
+  uint32_t od = out_deg[v];
+  t.activated += 1;
+  t.edges += od;
+  t.maxdeg = od > t.maxdeg ? od : t.maxdeg;
+  if (in_deg) t.in_edges += in_deg[v];
+  if (od > 0) q_out[atomicAdd(&st->next.qlen, 1u)] = v;
+}
+
+template <class Op, bool kUnique>
+__global__ void __launch_bounds__(SMALL_THREADS)
+    push_small(SmallRun *st, const uint32_t *__restrict__ q_in, uint32_t *__restrict__ q_out, Dir d, Op op,
+               uint32_t *stamp, uint32_t *visited, const uint32_t *__restrict__ out_deg,
+               const uint32_t *__restrict__ in_deg, unsigned long long *tr_ae, unsigned int *tr_act) {
+  __shared__ unsigned s_go, s_n, s_level, s_last;
+  if (threadIdx.x == 0) {
+    s_go = st->go;
+    s_n = st->n;
+    s_level = st->level;
+  }
+  __syncthreads();
+  if (!s_go) return;
+  const uint32_t n = s_n;
+  const unsigned level = s_level, lane = lane_id();
+  Tally t;
+  const size_t nround = ((size_t)n + 31) / 32 * 32;
+  for (size_t i = (size_t)blockIdx.x * SMALL_THREADS + threadIdx.x; i < nround; i += (size_t)gridDim.x * SMALL_THREADS) {
+    const bool valid = i < n;
+    uint32_t src = 0;
+    unsigned long long b = 0, e = 0;
+    if (valid) {
+      src = q_in[i];
+      b = d.off[src];
+      e = d.off[src + 1];
+    }
+    if (valid && e - b <= LIGHT_DEG) {
+      for (unsigned long long k = b; k < e; k++) {
+        uint32_t dst = d.nbr[k];
+        if (op.push(src, (uint32_t)i, dst, d.w ? d.w[k] : 0.0f))
+          small_activate<kUnique>(dst, st, stamp, level, visited, q_out, out_deg, in_deg, t);
+      }
+    }
+    unsigned coop = __ballot_sync(GG_FULL, valid && e - b > LIGHT_DEG);
+    while (coop) {
+      const unsigned leader = __ffs(coop) - 1;
+      coop &= coop - 1;
+      const unsigned long long lb = __shfl_sync(GG_FULL, b, leader), le = __shfl_sync(GG_FULL, e, leader);
+      const uint32_t lsrc = __shfl_sync(GG_FULL, src, leader);
+      const uint32_t li = (uint32_t)__shfl_sync(GG_FULL, (unsigned long long)i, leader);
+      for (unsigned long long k = lb + lane; k < le; k += 32) {
+        uint32_t dst = d.nbr[k];
+        if (op.push(lsrc, li, dst, d.w ? d.w[k] : 0.0f))
+          small_activate<kUnique>(dst, st, stamp, level, visited, q_out, out_deg, in_deg, t);
+      }
+    }
+  }
+  t.flush(&st->next);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long ne = atomicAdd(&st->next.edges, 0ull);
+    const unsigned int na = atomicAdd(&st->next.activated, 0u);
+    const unsigned int nq = atomicAdd(&st->next.qlen, 0u);
+    const unsigned int nm = atomicAdd(&st->next.maxdeg, 0u);
+    const unsigned int r = st->calls;
+    tr_ae[r] = st->ae;
+    tr_act[r] = na;
+    st->calls = r + 1;
+    st->total_ae += st->ae;
+    st->level = level + 1;
+    st->ae = ne;
+    st->n = nq;
+    st->last_activated = na;
+    st->next.edges = 0;
+    st->next.in_edges = 0;
+    st->next.activated = 0;
+    st->next.qlen = 0;
+    st->next.maxdeg = 0;
+    st->ticket = 0;
+    st->maxdeg = nm;
+    st->go = (na > 0 && ne < st->edges_lim && nq <= SMALL_MAX_QUEUE && ne <= SMALL_MAX_AE && nm <= SMALL_MAX_DEG)
+                 ? 1u
+                 : 0u;
+    __threadfence();
+  }
+}
+
+// Snapshot gather of a small call (CC, SSSP): msg[i] = src[q[i]].
+template <typename T>
+__global__ void small_gather(const SmallRun *st, const uint32_t *__restrict__ q, const T *__restrict__ src,
+                             T *__restrict__ msg) {
+  if (!st->go) return;
+  const uint32_t n = st->n;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    msg[i] = src[q[i]];
 }
 
 // ---------------------------------------------------------------- queue from bitmap
@@ -590,6 +737,78 @@ struct Launch {
     *n = *(uint32_t *)g->ws.ctr_host;
     return GG_OK;
   }
+  // Runs consecutive small sparse calls on the device (see SmallRun).  On
+  // entry q[*cur] holds the active vertices with out-degree > 0 (nq of them)
+  // and ae is the call's active_edges.  On return *cur, *nq, *ae describe the
+  // first call that did not run here and *n_act is the previous call's
+  // activated count; the trace has one row per call that ran.
+  template <class Op, bool kUnique, typename T>
+  int small_run(const Dir &d, const Op &op, uint32_t *q[2], int *cur, uint32_t *nq, unsigned long long *ae,
+                uint32_t *maxdeg, uint32_t *n_act, uint32_t *visited, const uint32_t *in_deg, const T *snap_src, T *snap_msg,
+                Trace &tr, uint32_t *stamp) {
+    SmallRun *st;
+    unsigned long long *tr_ae;
+    unsigned *tr_act;
+    char *blob;
+    const size_t st_bytes = 256, ae_bytes = sizeof(unsigned long long) * SMALL_BATCH;
+    GG_TRY(ws(g, WS_SMALL, st_bytes + ae_bytes + sizeof(unsigned) * SMALL_BATCH, &blob));
+    st = (SmallRun *)blob;
+    tr_ae = (unsigned long long *)(blob + st_bytes);
+    tr_act = (unsigned *)(blob + st_bytes + ae_bytes);
+    static thread_local std::vector<unsigned long long> h_ae;
+    static thread_local std::vector<unsigned> h_act;
+    h_ae.resize(SMALL_BATCH);
+    h_act.resize(SMALL_BATCH);
+    SmallRun h;
+    memset(&h, 0, sizeof(h));
+    h.ae = *ae;
+    h.edges_lim = g->E / 20;
+    h.n = *nq;
+    h.go = 1;
+    h.maxdeg = *maxdeg;
+    h.level = next_level();
+    cudaStream_t s = g->stream;
+    const unsigned grid = grid_for(SMALL_MAX_QUEUE, SMALL_THREADS, g->num_sms, 1);
+    // batches of 2, 4, 8, ... launches: a short run wastes few no-op launches
+    uint32_t batch = 2;
+    for (;;) {
+      GG_CUDA(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+      for (uint32_t i = 0; i < batch; i++) {
+        const int c = *cur ^ (int)(i & 1);
+        if (snap_msg) small_gather<T><<<grid, SMALL_THREADS, 0, s>>>(st, q[c], snap_src, snap_msg);
+        push_small<Op, kUnique><<<grid, SMALL_THREADS, 0, s>>>(st, q[c], q[c ^ 1], d, op, stamp, visited,
+                                                                d.deg, in_deg, tr_ae, tr_act);
+      }
+      launches += batch * (snap_msg ? 2 : 1);
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
+      GG_CUDA(cudaMemcpyAsync(h_ae.data(), tr_ae, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, s));
+      GG_CUDA(cudaMemcpyAsync(h_act.data(), tr_act, sizeof(unsigned) * batch, cudaMemcpyDeviceToHost, s));
+      GG_CUDA(cudaStreamSynchronize(s));
+      for (uint32_t r = 0; r < h.calls; r++) {
+        tr.add(0, h_ae[r], h_act[r]);
+        *n_act = h_act[r];
+      }
+      *cur ^= (int)(h.calls & 1);
+      level_ = h.level;
+      if (h.go) {  // the batch ended with the run still going
+        h.calls = 0;
+        batch = batch * 2 < SMALL_BATCH ? batch * 2 : SMALL_BATCH;
+        continue;
+      }
+      break;
+    }
+    *nq = h.n;
+    *ae = h.ae;
+    *maxdeg = h.maxdeg;
+    return GG_OK;
+  }
+  static bool small_ok(uint32_t nq, unsigned long long ae, uint32_t maxdeg) {
+    return ae > 0 && nq <= SMALL_MAX_QUEUE && ae <= SMALL_MAX_AE && maxdeg <= SMALL_MAX_DEG;
+  }
+  // Activation stamps grow across small runs of one graph; 0 marks "never".
+  unsigned level_ = 0;
+  unsigned next_level() { return level_ + 1; }
   int scan_queue_degrees(const uint32_t *q, uint32_t n, const uint32_t *deg, unsigned long long **P) {
     unsigned long long *p = nullptr, *scratch = nullptr;
     GG_TRY(ws(g, WS_PREFIX, (size_t)g->V + 2, &p));

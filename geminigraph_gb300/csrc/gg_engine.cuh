@@ -769,22 +769,55 @@ struct Launch {
     h.level = next_level();
     cudaStream_t s = g->stream;
     const unsigned grid = grid_for(SMALL_MAX_QUEUE, SMALL_THREADS, g->num_sms, 1);
-    // batches of 2, 4, 8, ... launches: a short run wastes few no-op launches
-    uint32_t batch = 2;
-    for (;;) {
-      GG_CUDA(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
-      for (uint32_t i = 0; i < batch; i++) {
+    // batches of 2, 4, 8, ... launches: a short run wastes few no-op launches;
+    // full batches of a long run replay one captured CUDA graph
+    auto enqueue = [&](uint32_t n) {
+      for (uint32_t i = 0; i < n; i++) {
         const int c = *cur ^ (int)(i & 1);
         if (snap_msg) small_gather<T><<<grid, SMALL_THREADS, 0, s>>>(st, q[c], snap_src, snap_msg);
         push_small<Op, kUnique><<<grid, SMALL_THREADS, 0, s>>>(st, q[c], q[c ^ 1], d, op, stamp, visited,
                                                                 d.deg, in_deg, tr_ae, tr_act);
       }
+    };
+    cudaGraphExec_t exec = nullptr;
+    int exec_parity = -1;
+    int status = GG_OK;
+    uint32_t batch = 2;
+    for (;;) {
+      cudaError_t e = cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess && batch == SMALL_BATCH) {
+        if (!exec || exec_parity != *cur) {
+          if (exec) cudaGraphExecDestroy(exec);
+          exec = nullptr;
+          cudaGraph_t graph = nullptr;
+          e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+          if (e == cudaSuccess) {
+            enqueue(batch);
+            e = cudaStreamEndCapture(s, &graph);
+          }
+          if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+          if (graph) cudaGraphDestroy(graph);
+          exec_parity = *cur;
+        }
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+      } else if (e == cudaSuccess) {
+        enqueue(batch);
+      }
+      if (e == cudaSuccess) e = cudaGetLastError();
+      if (e != cudaSuccess) {
+        status = cuda_status(e, "small run");
+        break;
+      }
       launches += batch * (snap_msg ? 2 : 1);
-      GG_CUDA(cudaGetLastError());
-      GG_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
-      GG_CUDA(cudaMemcpyAsync(h_ae.data(), tr_ae, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, s));
-      GG_CUDA(cudaMemcpyAsync(h_act.data(), tr_act, sizeof(unsigned) * batch, cudaMemcpyDeviceToHost, s));
-      GG_CUDA(cudaStreamSynchronize(s));
+      e = cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h_ae.data(), tr_ae, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h_act.data(), tr_act, sizeof(unsigned) * batch, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        status = cuda_status(e, "small run");
+        break;
+      }
       for (uint32_t r = 0; r < h.calls; r++) {
         tr.add(0, h_ae[r], h_act[r]);
         *n_act = h_act[r];
@@ -798,6 +831,8 @@ struct Launch {
       }
       break;
     }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (status != GG_OK) return status;
     *nq = h.n;
     *ae = h.ae;
     *maxdeg = h.maxdeg;

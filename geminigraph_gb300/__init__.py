@@ -78,6 +78,8 @@ def library():
         "gg_active_edges": ([vp, vp, ctypes.POINTER(u64)], i32),
         "gg_is_sparse": ([u64, u64], i32),
         "gg_active_edges_noalloc": ([vp, vp, u32, vp, vp], i32),
+        "gg_bfs_batched": ([vp, vp, i32, vp, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -301,6 +303,39 @@ class Graph:
         inv = np.empty(V, np.float64) if to_host else None
         _check(library().gg_bc(self.h, root, _ptr(dep), _ptr(inv), ctypes.byref(st.s)))
         return dep, inv, st
+
+
+def _roots_array(roots):
+    r = np.ascontiguousarray(roots, np.uint32)
+    if not 1 <= len(r) <= 64:
+        raise ValueError("1..64 roots per batch")
+    return r
+
+
+def bfs_batched(g, roots, levels=True, parents=False):
+    """Multi-source BFS of up to 64 roots: (levels, parents, reached, lane_edges, stats);
+    levels/parents are (len(roots), V) arrays or None."""
+    r = _roots_array(roots)
+    V = g.vertices
+    lv = np.empty((len(r), V), np.int32) if levels else None
+    pa = np.empty((len(r), V), np.uint32) if parents else None
+    reached = np.zeros(len(r), np.uint64)
+    edges = np.zeros(len(r), np.uint64)
+    st = RunStats()
+    _check(library().gg_bfs_batched(g.h, _ptr(r), len(r), _ptr(lv), _ptr(pa), _ptr(reached), _ptr(edges),
+                                    ctypes.byref(st.s)))
+    return lv, pa, reached, edges, st
+
+
+def sssp_batched(g, roots, distances=True):
+    """Multi-source SSSP of up to 64 roots: (distances (len(roots), V) or None, reached, stats)."""
+    r = _roots_array(roots)
+    V = g.vertices
+    dist = np.empty((len(r), V), np.float32) if distances else None
+    reached = np.zeros(len(r), np.uint64)
+    st = RunStats()
+    _check(library().gg_sssp_batched(g.h, _ptr(r), len(r), _ptr(dist), _ptr(reached), ctypes.byref(st.s)))
+    return dist, reached, st
 
 
 def pick_roots(out_degree, count, seed):

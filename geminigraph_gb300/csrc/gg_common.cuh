@@ -98,6 +98,10 @@ enum WsSlot {
   WS_QPOS,                              // per-word queue positions (queue_from_bitmap)
   WS_STAMP,                             // per-vertex activation stamps (small sparse runs)
   WS_SMALL,                             // SmallRun state and its trace rows
+  WS_MS_VISIT, WS_MS_FRONT, WS_MS_NEXT, // batched traversals: lane masks
+  WS_MS_LVL, WS_MS_PAR, WS_MS_DIST,     // batched traversals: per-lane state (vertex-major)
+  WS_MS_MISC, WS_MS_ROOTS,              // batched traversals: counters, roots
+  WS_MS_OUT0, WS_MS_OUT1,               // batched traversals: lane-major results
   WS_SCAN32,                            // scan scratch for 32-bit scans
   WS_NSLOTS
 };

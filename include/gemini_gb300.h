@@ -140,6 +140,22 @@ int gg_sssp(gg_graph *g, uint32_t root, float *distance, gg_run_stats *stats);
 int gg_bc(gg_graph *g, uint32_t root, double *dependencies, double *inv_num_paths,
           gg_run_stats *stats);
 
+/* ---- batched multi-source traversals (no counterpart in the reference) ----
+ * Up to 64 roots ("lanes") in one traversal; lane i's result equals gg_bfs /
+ * gg_sssp run alone on roots[i].  Results are lane-major host arrays
+ * (nroots * vertices entries, lane i at offset i * vertices); any may be NULL. */
+
+/* BFS: levels[i*V + v] = hop count from roots[i] (-1 if unreached); parents[i*V + v]
+ * = a BFS-tree parent (vertices if unreached); reached[i] = vertices reached;
+ * lane_edges[i] = the sum of active_edges a single-root run of roots[i] counts. */
+int gg_bfs_batched(gg_graph *g, const uint32_t *roots, int nroots, int32_t *levels, uint32_t *parents,
+                   uint64_t *reached, uint64_t *lane_edges, gg_run_stats *stats);
+
+/* SSSP on a weighted graph: distances[i*V + v] (1e9 if unreached), bit-identical
+ * to gg_sssp(g, roots[i]); reached[i] = vertices with distance < 1e9. */
+int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, float *distances, uint64_t *reached,
+                    gg_run_stats *stats);
+
 /* Device address of the last result of a toolkit kept on the device:
  * which = 0 primary output (parent / ranks / label / distance / dependencies),
  * 1 secondary (inv_num_paths).  Valid until the next toolkit call on g. */

@@ -1,0 +1,79 @@
+"""Batched multi-source BFS / SSSP: every lane must equal the single-root
+toolkit run on the same root (BFS levels identical, parents a valid tree and
+the same TEPS numerator; SSSP distances bit-identical)."""
+import numpy as np
+import pytest
+
+import geminigraph_gb300 as gg
+import graphgen
+from golden_util import Fixture
+from oracle.oracle import bfs_levels
+
+pytestmark = pytest.mark.gpu
+
+
+def graphs():
+    s, d, w = graphgen.rmat(15, 16, 21, weighted=True)
+    yield "rmat15", 1 << 15, s, d, w
+    s, d, w = graphgen.grid(64, seed=3, weighted=True)
+    yield "grid64", 64 * 64, s, d, w
+    fx = Fixture("edgecase")
+    yield "edgecase", fx.V, fx.src, fx.dst, fx.w
+
+
+@pytest.fixture(scope="module", params=list(graphs()), ids=lambda p: p[0])
+def case(request):
+    name, V, s, d, w = request.param
+    return V, s, d, w, gg.Graph.from_edges(V, s, d, w)
+
+
+def roots_for(V, s, n, seed):
+    deg = np.bincount(s, minlength=V)
+    roots = gg.pick_roots(deg, n, seed)
+    roots[1] = roots[0]                              # a duplicated root
+    zero = np.nonzero(deg == 0)[0]
+    if len(zero):
+        roots[2] = int(zero[0])                      # a root with no out-edges
+    return roots
+
+
+@pytest.mark.parametrize("n", [1, 7, 64])
+def test_bfs_batched_lanes_equal_single_runs(case, n):
+    V, s, d, w, g = case
+    roots = roots_for(V, s, max(n, 3), seed=n)[:n]
+    lv, pa, reached, edges, st = gg.bfs_batched(g, roots, levels=True, parents=True)
+    for i, r in enumerate(roots):
+        parent, single = g.bfs(r)
+        ref = bfs_levels(parent, r)
+        assert np.array_equal(lv[i], ref), f"lane {i} root {r}"
+        assert np.array_equal(bfs_levels(pa[i], r), ref)
+        ok = pa[i] < V
+        ok[r] = False
+        src = pa[i][ok].astype(np.int64)
+        dst = np.nonzero(ok)[0]
+        have = set(zip(s.tolist(), d.tolist()))
+        assert all((int(a), int(b)) in have for a, b in zip(src, dst))
+        assert int(reached[i]) == int((parent < V).sum())
+        assert int(edges[i]) == single.active_edges_total
+
+
+@pytest.mark.parametrize("n", [1, 13, 64])
+def test_sssp_batched_lanes_equal_single_runs(case, n):
+    V, s, d, w, g = case
+    roots = roots_for(V, s, max(n, 3), seed=100 + n)[:n]
+    dist, reached, st = gg.sssp_batched(g, roots)
+    for i, r in enumerate(roots):
+        single, _ = g.sssp(r)
+        assert np.array_equal(dist[i].view(np.uint32), single.view(np.uint32)), f"lane {i} root {r}"
+        assert int(reached[i]) == int((single < np.float32(1e9)).sum())
+
+
+def test_batched_argument_errors(case):
+    V, s, d, w, g = case
+    with pytest.raises(ValueError):
+        gg.bfs_batched(g, list(range(65)))
+    with pytest.raises(gg.GeminiError):
+        gg.bfs_batched(g, [V])
+    gu = gg.Graph.from_edges(V, s, d)
+    with pytest.raises(gg.GeminiError):
+        gg.sssp_batched(gu, [0])

@@ -57,8 +57,14 @@ WORKLOADS = {
                desc="BC (double) from seeded roots on R-MAT scale 25, edge factor 16"),
     "bfs_grid": dict(kind="grid", scale=8192, ef=0, weighted=False, symmetric=False,
                      desc="BFS on the 8192 x 8192 4-neighbour grid (both directions)"),
+    "bfs_batched": dict(kind="rmat", scale=24, ef=16, weighted=False, symmetric=False,
+                        desc="batched BFS, 64 seeded roots per launch, on directed R-MAT scale 24, edge factor 16"),
+    "sssp_batched": dict(kind="rmat", scale=24, ef=16, weighted=True, symmetric=False,
+                         desc="batched SSSP, 64 seeded roots per launch, on R-MAT scale 24, edge factor 16, "
+                              "float weights in [0,1)"),
 }
-REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs"}
+REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs",
+           "bfs_batched": "bfs", "sssp_batched": "sssp"}
 
 
 def log(*a):
@@ -228,7 +234,8 @@ def step_args(gg, g, workload, count):
 
 # ----------------------------------------------------------------- CPU side
 def ref_sample_scale(workload):
-    return {"bfs": 22, "cc": 21, "pagerank": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024}[workload]
+    return {"bfs": 22, "cc": 21, "pagerank": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024, "bfs_batched": 22,
+            "sssp_batched": 21}[workload]
 
 
 def cpu_reference(gg, workload, nsteps, warmup):
@@ -250,7 +257,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
     src, dst = words[:, 0].copy(), words[:, 1].copy()
     wts = words[:, 2].view(np.float32).copy() if w["weighted"] else None
     n = warmup + nsteps
-    if workload in ("bfs", "sssp", "bc"):
+    if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched"):
         args = gg.pick_roots(np.bincount(src, minlength=V), n, seed=SEED + 2000)
     elif workload == "bfs_grid":
         args = [0] * n
@@ -262,9 +269,9 @@ def cpu_reference(gg, workload, nsteps, warmup):
     og = OracleGraph(V, src, dst, wts, symmetric=w["symmetric"])
     numer = []
     for a in args:
-        if workload in ("bfs", "bfs_grid"):
+        if workload in ("bfs", "bfs_grid", "bfs_batched"):
             tr = og.bfs(a)[1]
-        elif workload == "sssp":
+        elif workload in ("sssp", "sssp_batched"):
             tr = og.sssp(a)[1]
         elif workload == "bc":
             tr = og.bc(a)[2]
@@ -297,9 +304,9 @@ def cpu_reference(gg, workload, nsteps, warmup):
     t, e = [], []
     for i, a in enumerate(args):
         t0 = time.perf_counter()
-        if workload in ("bfs", "bfs_grid"):
+        if workload in ("bfs", "bfs_grid", "bfs_batched"):
             og.bfs(a)
-        elif workload == "sssp":
+        elif workload in ("sssp", "sssp_batched"):
             og.sssp(a)
         elif workload == "bc":
             og.bc(a)
@@ -435,6 +442,90 @@ def gpu_arm(args, dist):
     return 0
 
 
+def gpu_arm_batched(args, dist):
+    """One step = one batch of 64 roots.  value = queries/s of the batched
+    kernel; plain = the same roots one at a time through gg_bfs / gg_sssp."""
+    import geminigraph_gb300 as gg
+    w = WORKLOADS[args.workload]
+    device = dist.local_rank
+    t0 = time.perf_counter()
+    g = make_graph(gg, w, device)
+    build_s = time.perf_counter() - t0
+    info = g.info()
+    V = info["vertices"]
+    bfs = args.workload == "bfs_batched"
+    lanes = 64
+    roots = gg.pick_roots(g.out_degree(), lanes * (args.warmup + 2 * args.steps), seed=SEED + 3000)
+    batches = [roots[i * lanes:(i + 1) * lanes] for i in range(args.warmup + 2 * args.steps)]
+
+    def run_batch(rs, host):
+        if bfs:
+            _, _, _, edges, st = gg.bfs_batched(g, rs, levels=host, parents=False, timing=True)
+            return st, int(edges.sum())
+        _, _, st = gg.sssp_batched(g, rs, distances=host, timing=True)
+        return st, 0
+
+    for b in batches[:args.warmup]:
+        run_batch(b, False)
+    clocks = ClockSampler(device)
+    clocks.start()
+    dist.barrier()
+    dev_ms, edges, launches = 0.0, 0, 0
+    first = None
+    for b in batches[args.warmup:args.warmup + args.steps]:
+        st, e = run_batch(b, False)
+        dev_ms += st.device_ms
+        edges += e
+        launches += st.kernel_launches
+        first = first or st
+    dist.barrier()
+    clk = clocks.stop()
+    t_max = dist.max(dev_ms / 1000.0)
+    q_all = dist.sum(lanes * args.steps)
+    value = q_all / t_max
+    # plain: the same number of roots one at a time (device time)
+    plain_ms = 0.0
+    plain_roots = [r for b in batches[args.warmup:args.warmup + args.steps] for r in b][:lanes]
+    for r in plain_roots:
+        if bfs:
+            _, st = g.bfs(r, to_host=False)
+        else:
+            _, st = g.sssp(r, to_host=False)
+        plain_ms += st.device_ms
+    plain_qps = len(plain_roots) / (plain_ms / 1000.0)
+    # e2e: per-lane results copied to host memory
+    dist.barrier()
+    e_wall = 0.0
+    for b in batches[args.warmup + args.steps:]:
+        t1 = time.perf_counter()
+        run_batch(b, True)
+        e_wall += time.perf_counter() - t1
+    e_max = dist.max(e_wall)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_max * 1000 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 lane masks" if bfs else "f32",
+        "data": "synthetic (seeded R-MAT generated on the device)",
+        "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"], "lanes": lanes,
+                   "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
+                   "l2": "inputs larger than L2"},
+        "plain": {"value": round(plain_qps, 1), "unit": "queries/s",
+                  "what": f"{len(plain_roots)} roots one at a time through the single-root kernels (device time)"},
+        "speedup_vs_plain": round(value / plain_qps, 2),
+        "e2e": {"value": round(dist.sum(lanes * args.steps) / e_max, 1), "unit": "queries/s",
+                "h2d_bytes_per_step": 4 * lanes, "d2h_bytes_per_step": 4 * lanes * V,
+                "ms_per_step": round(e_max * 1000 / args.steps, 3)},
+        "gpu_launches": launches, "clocks": clk,
+        "trace_first_step": [list(r) for r in first.rows(with_ms=True)[:60]] if first else [],
+    }
+    if bfs:
+        line["lane_gteps"] = round(dist.sum(edges) / t_max / 1e9, 2)
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    return 0
+
+
 def run_once_stats(gg, g, workload, a, st):
     L = gg.library()
     import ctypes
@@ -491,6 +582,8 @@ def main():
     try:
         if args.impl == "reference":
             return reference_arm(args, dist)
+        if args.workload.endswith("_batched"):
+            return gpu_arm_batched(args, dist)
         return gpu_arm(args, dist)
     finally:
         dist.close()

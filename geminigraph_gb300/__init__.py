@@ -79,6 +79,15 @@ def library():
         "gg_is_sparse": ([u64, u64], i32),
         "gg_active_edges_noalloc": ([vp, vp, u32, vp, vp], i32),
         "gg_bfs_batched": ([vp, vp, i32, vp, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
+        "gg_result_checksum": ([vp, u32, i32], u64),
+        "gg_levels_from_parents": ([vp, u32, u32, vp], i32),
+        "gg_server_create": ([i32, u64, pg], i32),
+        "gg_server_add_graph": ([vp, vp, ctypes.POINTER(i32)], i32),
+        "gg_server_submit": ([vp, i32, i32, u32, ctypes.POINTER(u64)], i32),
+        "gg_server_wait": ([vp, ctypes.POINTER(_QueryResult), i32, i32, ctypes.POINTER(i32)], i32),
+        "gg_server_stats_get": ([vp, ctypes.POINTER(_ServerStats)], i32),
+        "gg_server_free": ([vp], i32),
+        "gg_pool_bytes": ([vp, i32], u64),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
     for name, (args, res) in sig.items():
@@ -96,6 +105,19 @@ def _check(rc):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _QueryResult(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_uint64), ("graph", ctypes.c_int32), ("kind", ctypes.c_int32),
+                ("root", ctypes.c_uint32), ("status", ctypes.c_int32), ("reached", ctypes.c_uint64),
+                ("checksum", ctypes.c_uint64), ("active_edges", ctypes.c_uint64), ("latency_ms", ctypes.c_double)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("pending", ctypes.c_uint64), ("pools_open", ctypes.c_uint64),
+                ("pools_opened", ctypes.c_uint64), ("pools_closed", ctypes.c_uint64),
+                ("admission_waits", ctypes.c_uint64), ("bytes_in_use", ctypes.c_uint64), ("budget", ctypes.c_uint64),
+                ("max_busy_pools", ctypes.c_int32), ("max_lanes_in_use", ctypes.c_int32)]
 
 
 class RunStats:
@@ -132,8 +154,11 @@ class RunStats:
     def kernel_launches(self):
         return self.s.kernel_launches
 
-    def rows(self):
+    def rows(self, with_ms=False):
         n = min(self.s.calls, len(self.mode))
+        if with_ms and self.call_ms is not None:
+            return [(int(self.mode[i]), int(self.active_edges[i]), int(self.activated[i]),
+                     round(float(self.call_ms[i]), 4)) for i in range(n)]
         return [(int(self.mode[i]), int(self.active_edges[i]), int(self.activated[i])) for i in range(n)]
 
 
@@ -312,7 +337,7 @@ def _roots_array(roots):
     return r
 
 
-def bfs_batched(g, roots, levels=True, parents=False):
+def bfs_batched(g, roots, levels=True, parents=False, timing=False):
     """Multi-source BFS of up to 64 roots: (levels, parents, reached, lane_edges, stats);
     levels/parents are (len(roots), V) arrays or None."""
     r = _roots_array(roots)
@@ -322,20 +347,85 @@ def bfs_batched(g, roots, levels=True, parents=False):
     reached = np.zeros(len(r), np.uint64)
     edges = np.zeros(len(r), np.uint64)
     st = RunStats()
+    if timing:
+        st.enable_call_timing()
     _check(library().gg_bfs_batched(g.h, _ptr(r), len(r), _ptr(lv), _ptr(pa), _ptr(reached), _ptr(edges),
                                     ctypes.byref(st.s)))
     return lv, pa, reached, edges, st
 
 
-def sssp_batched(g, roots, distances=True):
+def sssp_batched(g, roots, distances=True, timing=False):
     """Multi-source SSSP of up to 64 roots: (distances (len(roots), V) or None, reached, stats)."""
     r = _roots_array(roots)
     V = g.vertices
     dist = np.empty((len(r), V), np.float32) if distances else None
     reached = np.zeros(len(r), np.uint64)
     st = RunStats()
+    if timing:
+        st.enable_call_timing()
     _check(library().gg_sssp_batched(g.h, _ptr(r), len(r), _ptr(dist), _ptr(reached), ctypes.byref(st.s)))
     return dist, reached, st
+
+
+def result_checksum(values, kind):
+    """gg_result_checksum of a level (kind 0, int32) or distance (kind 1, float32) array."""
+    a = np.ascontiguousarray(values, np.int32 if kind == 0 else np.float32)
+    return int(library().gg_result_checksum(_ptr(a), len(a), kind))
+
+
+def levels_from_parents(parent, root):
+    p = np.ascontiguousarray(parent, np.uint32)
+    lv = np.empty(len(p), np.int32)
+    _check(library().gg_levels_from_parents(_ptr(p), len(p), root, _ptr(lv)))
+    return lv
+
+
+class Server:
+    """Continuous-batching BFS/SSSP server over resident graphs (gg_server_*)."""
+    BFS, SSSP = 0, 1
+
+    def __init__(self, device=0, hbm_budget=0):
+        h = ctypes.c_void_p()
+        _check(library().gg_server_create(device, hbm_budget, ctypes.byref(h)))
+        self.h = h
+        self.graphs = []
+
+    @staticmethod
+    def pool_bytes(graph, kind):
+        return int(library().gg_pool_bytes(graph.h, kind))
+
+    def add_graph(self, graph):
+        gid = ctypes.c_int32()
+        _check(library().gg_server_add_graph(self.h, graph.h, ctypes.byref(gid)))
+        self.graphs.append(graph)
+        return gid.value
+
+    def submit(self, graph_id, kind, root):
+        t = ctypes.c_uint64()
+        _check(library().gg_server_submit(self.h, graph_id, kind, root, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, max_results=256, timeout_ms=100):
+        buf = (_QueryResult * max_results)()
+        n = ctypes.c_int32()
+        _check(library().gg_server_wait(self.h, buf, max_results, timeout_ms, ctypes.byref(n)))
+        return [{k: getattr(buf[i], k) for k, _ in _QueryResult._fields_} for i in range(n.value)]
+
+    def stats(self):
+        st = _ServerStats()
+        _check(library().gg_server_stats_get(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            library().gg_server_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def pick_roots(out_degree, count, seed):

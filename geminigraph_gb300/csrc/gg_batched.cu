@@ -18,18 +18,15 @@
 #include <vector>
 
 #include "gg_engine.cuh"
+#include "gg_gen.h"
+#include "gg_lanes.cuh"
 
 namespace gg {
 
 typedef unsigned long long u64;
 constexpr int LANES = 64;
 
-struct MsCounters {
-  u64 alive;           // OR of the lanes activated this iteration
-  u64 edges;           // sum of out_degree over vertices touched this iteration
-  unsigned int touched;
-  unsigned int qlen;
-};
+typedef LaneCounters MsCounters;
 
 // write_min on a float (core/atomic.hpp:35-42): true if this call lowered *p.
 __device__ __forceinline__ bool atomic_min_float_b(float *p, float v) {
@@ -85,28 +82,6 @@ __device__ __forceinline__ void ms_record(uint32_t v, u64 bits, uint32_t u, uint
     lvl[(size_t)v * LANES + l] = iter;
     if (par) par[(size_t)v * LANES + l] = u;
   }
-}
-
-__global__ void ms_roots(const uint32_t *roots, int n, u64 *front, u64 *visit, uint32_t *lvl, uint32_t *par,
-                         uint32_t iter, const uint32_t *out_deg, MsCounters *mc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  u64 alive = 0, edges = 0;
-  unsigned touched = 0;
-  for (int l = 0; l < n; l++) {
-    uint32_t r = roots[l];
-    if (!front[r]) {
-      edges += out_deg[r];
-      touched += 1;
-    }
-    front[r] |= 1ull << l;
-    visit[r] |= 1ull << l;
-    lvl[(size_t)r * LANES + l] = iter;
-    if (par) par[(size_t)r * LANES + l] = r;
-    alive |= 1ull << l;
-  }
-  mc->alive = alive;
-  mc->edges = edges;
-  mc->touched = touched;
 }
 
 // ---------------------------------------------------------------- BFS pull
@@ -282,250 +257,149 @@ __global__ void ms_compact(const u64 *__restrict__ m, uint32_t V, const uint32_t
     if (m[v]) q[pos[v]] = (uint32_t)v;
 }
 
-// Per-lane results in the caller's layout (lane-major), through a shared
-// tile of 32 vertices x 64 lanes; also per-lane reached counts and edge sums.
+
+// ---------------------------------------------------------------- pool kernels
+// visit[v] &= ~mask: lanes about to be reused start unvisited everywhere.
+__global__ void lanes_reset_visit(u64 *visit, uint32_t V, u64 mask) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    visit[v] &= ~mask;
+}
+
+// dist[v][l] = 1e9 for the lanes in mask.
+__global__ void lanes_reset_dist(float *dist, uint32_t V, u64 mask) {
+  const size_t n = (size_t)V * LANES;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if ((mask >> (i % LANES)) & 1ull) dist[i] = 1e9f;
+}
+
+// Roots into lanes: frontier bit, visited bit / distance 0, discovery iteration.
+__global__ void lanes_admit(const uint32_t *roots, const int *lanes, int n, u64 *front, u64 *visit, uint32_t *lvl,
+                            uint32_t *par, float *dist, uint32_t iter, const uint32_t *out_deg, MsCounters *mc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  u64 edges = 0;
+  for (int i = 0; i < n; i++) {
+    const uint32_t r = roots[i];
+    const int l = lanes[i];
+    if (!front[r]) edges += out_deg[r];
+    front[r] |= 1ull << l;
+    if (visit) visit[r] |= 1ull << l;
+    if (lvl) lvl[(size_t)r * LANES + l] = iter;
+    if (par) par[(size_t)r * LANES + l] = r;
+    if (dist) dist[(size_t)r * LANES + l] = 0.0f;
+  }
+  mc->edges = edges;
+}
+
+// Checksum term of one result entry (matches gg_result_checksum).
+__device__ __forceinline__ u64 result_term(uint32_t v, uint32_t x) {
+  return gg_mix64((u64)v * 0x9E3779B97F4A7C15ull + x);
+}
+
+// Per-lane digests of the lanes in mask: out[l] reached, out[64+l] checksum,
+// out[128+l] out-degree sum of reached vertices.  BFS: x = hop count; SSSP:
+// x = the distance's float bits.  One warp per 32 vertices; lane j of the
+// warp keeps traversal lanes j and j + 32.
 __global__ void __launch_bounds__(256)
-    ms_extract(uint32_t V, int n, const u64 *__restrict__ visit, const uint32_t *__restrict__ lvl,
-               const uint32_t *__restrict__ par, const uint32_t *__restrict__ out_deg, int32_t *levels,
-               uint32_t *parents, u64 *reached, u64 *edges) {
-  __shared__ uint32_t s_lvl[32][LANES + 1];
-  __shared__ uint32_t s_par[32][LANES + 1];
-  __shared__ u64 s_vis[32];
-  __shared__ uint32_t s_deg[32];
-  __shared__ u64 s_reach[LANES], s_edge[LANES];
-  if (threadIdx.x < LANES) {
-    s_reach[threadIdx.x] = 0;
-    s_edge[threadIdx.x] = 0;
+    lanes_digest(uint32_t V, u64 mask, const u64 *__restrict__ visit, const uint32_t *__restrict__ lvl,
+                 const uint32_t *__restrict__ start, const float *__restrict__ dist,
+                 const uint32_t *__restrict__ out_deg, u64 *out) {
+  __shared__ u64 s_out[3 * LANES];
+  for (int i = threadIdx.x; i < 3 * LANES; i += blockDim.x) s_out[i] = 0;
+  __syncthreads();
+  const unsigned lane = lane_id();
+  u64 acc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+  const size_t nwarps = (size_t)gridDim.x * 8;
+  for (size_t g = (size_t)blockIdx.x * 8 + (threadIdx.x >> 5); g * 32 < V; g += nwarps) {
+    const size_t v = g * 32 + lane;
+    const bool in = v < V;
+    const uint32_t dg = in ? out_deg[v] : 0u;
+    u64 vm = 0;
+    if (visit) vm = in ? visit[v] & mask : 0ull;
+    if (visit && !__any_sync(GG_FULL, vm != 0)) continue;
+    u64 rest = mask;
+    while (rest) {
+      const int l = __ffsll((long long)rest) - 1;
+      rest &= rest - 1;
+      bool hit;
+      uint32_t x = 0;
+      if (visit) {
+        hit = (vm >> l) & 1ull;
+        if (hit) x = lvl[v * LANES + l] - start[l];
+      } else {
+        const float dv = in ? dist[v * LANES + l] : 1e9f;
+        hit = dv < 1e9f;
+        x = __float_as_uint(dv);
+      }
+      const unsigned cnt = __popc(__ballot_sync(GG_FULL, hit));
+      const u64 h = warp_sum(hit ? result_term((uint32_t)v, x) : 0ull);
+      const unsigned lo = __reduce_add_sync(GG_FULL, hit ? (dg & 0xffffu) : 0u);
+      const unsigned hi = __reduce_add_sync(GG_FULL, hit ? (dg >> 16) : 0u);
+      if ((unsigned)(l & 31) == lane) {
+        u64 *a = acc[l >> 5];
+        a[0] += cnt;
+        a[1] += h;
+        a[2] += (u64)lo + ((u64)hi << 16);
+      }
+    }
+  }
+  for (int half = 0; half < 2; half++) {
+    const int l = (int)lane + 32 * half;
+    if ((mask >> l) & 1ull) {
+      atomicAdd(&s_out[l], acc[half][0]);
+      atomicAdd(&s_out[LANES + l], acc[half][1]);
+      atomicAdd(&s_out[2 * LANES + l], acc[half][2]);
+    }
   }
   __syncthreads();
+  for (int i = threadIdx.x; i < 3 * LANES; i += blockDim.x)
+    if (s_out[i]) atomicAdd(&out[i], s_out[i]);
+}
+
+// Lane-major results of lanes[0..n): levels[j*V + v] (hop count or -1),
+// parents[j*V + v] (or V), dist_out[j*V + v], through a shared tile of 32
+// vertices x n lanes.
+__global__ void __launch_bounds__(256)
+    lanes_extract(uint32_t V, const int *lanes, int n, const u64 *__restrict__ visit, const uint32_t *__restrict__ lvl,
+                  const uint32_t *__restrict__ start, const uint32_t *__restrict__ par, const float *__restrict__ dist,
+                  int32_t *levels, uint32_t *parents, float *dist_out) {
+  __shared__ uint32_t s_a[32][LANES + 1];
+  __shared__ uint32_t s_b[32][LANES + 1];
+  __shared__ u64 s_vis[32];
+  __shared__ int s_lane[LANES];
+  if (threadIdx.x < (unsigned)n) s_lane[threadIdx.x] = lanes[threadIdx.x];
+  __syncthreads();
   for (size_t v0 = (size_t)blockIdx.x * 32; v0 < V; v0 += (size_t)gridDim.x * 32) {
-    for (int i = threadIdx.x; i < 32 * LANES; i += blockDim.x) {
-      const int r = i / LANES, l = i % LANES;
+    for (int i = threadIdx.x; i < 32 * n; i += blockDim.x) {
+      const int r = i / n, j = i % n;
       const size_t v = v0 + r;
-      if (v < V) {
-        s_lvl[r][l] = lvl[v * LANES + l];
-        if (par) s_par[r][l] = par[v * LANES + l];
-      }
+      if (v >= V) continue;
+      const int l = s_lane[j];
+      if (levels) s_a[r][j] = lvl[v * LANES + l] - start[l];
+      if (parents) s_b[r][j] = par[v * LANES + l];
+      if (dist_out) s_a[r][j] = __float_as_uint(dist[v * LANES + l]);
     }
     if (threadIdx.x < 32) {
       const size_t v = v0 + threadIdx.x;
-      s_vis[threadIdx.x] = v < V ? visit[v] : 0ull;
-      s_deg[threadIdx.x] = v < V ? out_deg[v] : 0u;
+      s_vis[threadIdx.x] = (visit && v < V) ? visit[v] : 0ull;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 32 * n; i += blockDim.x) {
-      const int l = i / 32, r = i % 32;
+      const int j = i / 32, r = i % 32;
       const size_t v = v0 + r;
       if (v >= V) continue;
-      const bool hit = (s_vis[r] >> l) & 1ull;
-      if (levels) levels[(size_t)l * V + v] = hit ? (int32_t)s_lvl[r][l] : -1;
-      if (parents) parents[(size_t)l * V + v] = hit ? s_par[r][l] : V;
-      if (hit) {
-        atomicAdd(&s_reach[l], 1ull);
-        atomicAdd(&s_edge[l], (u64)s_deg[r]);
+      if (dist_out) {
+        dist_out[(size_t)j * V + v] = __uint_as_float(s_a[r][j]);
+        continue;
       }
+      const bool hit = (s_vis[r] >> s_lane[j]) & 1ull;
+      if (levels) levels[(size_t)j * V + v] = hit ? (int32_t)s_a[r][j] : -1;
+      if (parents) parents[(size_t)j * V + v] = hit ? s_b[r][j] : V;
     }
     __syncthreads();
   }
-  if (threadIdx.x < (unsigned)n) {
-    if (s_reach[threadIdx.x]) atomicAdd(&reached[threadIdx.x], s_reach[threadIdx.x]);
-    if (s_edge[threadIdx.x]) atomicAdd(&edges[threadIdx.x], s_edge[threadIdx.x]);
-  }
-}
-
-}  // namespace gg
-
-using namespace gg;
-
-namespace {
-
-struct BatchBuffers {
-  u64 *visit, *front, *next;
-  uint32_t *lvl, *par, *q[2];
-  MsCounters *mc;
-  u64 *lane_reached, *lane_edges;
-};
-
-int ms_buffers(gg_graph *g, bool want_par, BatchBuffers *b) {
-  const uint32_t V = g->V;
-  GG_TRY(ws(g, WS_MS_VISIT, V, &b->visit));
-  GG_TRY(ws(g, WS_MS_FRONT, V, &b->front));
-  GG_TRY(ws(g, WS_MS_NEXT, V, &b->next));
-  GG_TRY(ws(g, WS_MS_LVL, (size_t)V * LANES, &b->lvl));
-  b->par = nullptr;
-  if (want_par) GG_TRY(ws(g, WS_MS_PAR, (size_t)V * LANES, &b->par));
-  GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &b->q[0]));
-  GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &b->q[1]));
-  char *blob;
-  GG_TRY(ws(g, WS_MS_MISC, 256 + sizeof(u64) * 2 * LANES, &blob));
-  b->mc = (MsCounters *)blob;
-  b->lane_reached = (u64 *)(blob + 256);
-  b->lane_edges = b->lane_reached + LANES;
-  return GG_OK;
-}
-
-int ms_read(gg_graph *g, MsCounters *mc, MsCounters *h) {
-  GG_CUDA(cudaMemcpyAsync(g->ws.ctr_host, mc, sizeof(MsCounters), cudaMemcpyDeviceToHost, g->stream));
-  GG_CUDA(cudaStreamSynchronize(g->stream));
-  memcpy(h, g->ws.ctr_host, sizeof(MsCounters));
-  return GG_OK;
-}
-
-}  // namespace
-
-extern "C" int gg_bfs_batched(gg_graph *g, const uint32_t *roots, int nroots, int32_t *levels, uint32_t *parents,
-                              uint64_t *reached, uint64_t *lane_edges, gg_run_stats *stats) {
-  if (!g || !roots || nroots < 1 || nroots > LANES) {
-    set_error("need a graph and 1..64 roots");
-    return GG_ERR_INVALID;
-  }
-  for (int i = 0; i < nroots; i++)
-    if (roots[i] >= g->V) {
-      set_error("root %u >= vertices %u", roots[i], g->V);
-      return GG_ERR_INVALID;
-    }
-  GG_CUDA(cudaSetDevice(g->device));
-  const uint32_t V = g->V;
-  BatchBuffers b;
-  GG_TRY(ms_buffers(g, parents != nullptr, &b));
-  Launch L(g);
-  Trace tr(stats, g);
-  cudaStream_t s = g->stream;
-  uint32_t *d_roots;
-  GG_TRY(ws(g, WS_MS_ROOTS, LANES, &d_roots));
-  GG_TRY(timed_begin(g));
-  GG_CUDA(cudaMemcpyAsync(d_roots, roots, sizeof(uint32_t) * nroots, cudaMemcpyHostToDevice, s));
-  GG_CUDA(cudaMemsetAsync(b.visit, 0, sizeof(u64) * V, s));
-  GG_CUDA(cudaMemsetAsync(b.front, 0, sizeof(u64) * V, s));
-  GG_CUDA(cudaMemsetAsync(b.mc, 0, 256 + sizeof(u64) * 2 * LANES, s));
-  ms_roots<<<1, 32, 0, s>>>(d_roots, nroots, b.front, b.visit, b.lvl, b.par, 0, g->out.deg, b.mc);
-  L.launches += 1;
-  GG_CUDA(cudaGetLastError());
-  MsCounters h;
-  GG_TRY(ms_read(g, b.mc, &h));
-  // queue of the union frontier, when the next iteration pushes
-  {
-    uint32_t *pos, *scratch;
-    GG_TRY(ws(g, WS_QPOS, (size_t)V + 1, &pos));
-    GG_TRY(ws(g, WS_SCAN32, scan_scratch_elems(V), &scratch));
-    GG_CUDA((exclusive_scan<uint32_t, NonzeroMask>(NonzeroMask{b.front}, V, pos, scratch, s, &L.launches)));
-    ms_compact<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(b.front, V, pos, b.q[0]);
-    L.launches += 1;
-  }
-  uint32_t nq = h.touched;
-  bool qvalid = true;
-  u64 alive = h.alive;
-  unsigned long long ae = h.edges;
-  int cur = 0;
-  bool next_clear = false;  // next[] is all zero
-  for (uint32_t iter = 1; alive; iter++) {
-    const bool sparse = ae < g->E / 20;
-    tr.add(sparse ? 0 : 1, ae, 0);
-    GG_CUDA(cudaMemsetAsync(b.mc, 0, sizeof(MsCounters), s));
-    if (sparse) {
-      if (!qvalid) {
-        uint32_t *pos, *scratch;
-        GG_TRY(ws(g, WS_QPOS, (size_t)V + 1, &pos));
-        GG_TRY(ws(g, WS_SCAN32, scan_scratch_elems(V), &scratch));
-        GG_CUDA((exclusive_scan<uint32_t, NonzeroMask>(NonzeroMask{b.front}, V, pos, scratch, s, &L.launches)));
-        ms_compact<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(b.front, V, pos, b.q[cur]);
-        GG_CUDA(cudaMemcpyAsync(g->ws.ctr_host, pos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        GG_CUDA(cudaStreamSynchronize(s));
-        nq = *(uint32_t *)g->ws.ctr_host;
-        L.launches += 1;
-      }
-      if (!next_clear) GG_CUDA(cudaMemsetAsync(b.next, 0, sizeof(u64) * V, s));
-      if (ae > 0) {
-        unsigned long long *P;
-        GG_TRY(L.scan_queue_degrees(b.q[cur], nq, g->out.deg, &P));
-        GG_TRY(tr.kbegin());
-        ms_push<<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(b.q[cur], P, nq, ae, g->out, b.front, b.visit, b.next, b.lvl,
-                                                          b.par, iter, b.q[cur ^ 1], b.mc);
-        GG_TRY(tr.kend());
-        L.launches += 1;
-      }
-      MsCounters hq;
-      GG_TRY(ms_read(g, b.mc, &hq));
-      if (hq.qlen)
-        ms_push_finish<<<grid_for(hq.qlen, 256, g->num_sms), 256, 0, s>>>(b.q[cur ^ 1], hq.qlen, b.visit, b.next,
-                                                                         g->out.deg, b.mc);
-      // the old frontier becomes next: clear it through its queue
-      ms_clear_queue<<<grid_for(nq ? nq : 1, 256, g->num_sms), 256, 0, s>>>(b.q[cur], nq, b.front);
-      L.launches += 2;
-      GG_TRY(ms_read(g, b.mc, &h));
-      nq = h.qlen;
-      qvalid = true;
-      cur ^= 1;
-      next_clear = true;
-    } else {
-      GG_TRY(tr.kbegin());
-      ms_pull_light<<<L.pull_grid(), 256, 0, s>>>(g->in, V, alive, b.front, b.visit, b.next, b.lvl, b.par, iter,
-                                                  g->out.deg, b.mc);
-      L.launches += 1;
-      if (g->in.nbig) {
-        ms_pull_chunks<<<grid_for((size_t)g->in.nbigchunks * 32, 256, g->num_sms, 8), 256, 0, s>>>(
-            g->in, alive, b.front, b.visit, b.next, b.lvl, b.par, iter);
-        ms_big_finish<<<grid_for(g->in.nbig, 256, g->num_sms), 256, 0, s>>>(g->in, b.visit, b.next, g->out.deg,
-                                                                          b.mc);
-        L.launches += 2;
-      }
-      GG_TRY(tr.kend());
-      GG_TRY(ms_read(g, b.mc, &h));
-      qvalid = false;
-      next_clear = false;
-    }
-    GG_CUDA(cudaGetLastError());
-    tr.set_activated(h.touched);
-    alive = h.alive;
-    ae = h.edges;
-    u64 *t = b.front;
-    b.front = b.next;
-    b.next = t;
-  }
-  GG_CUDA(cudaMemsetAsync(b.lane_reached, 0, sizeof(u64) * 2 * LANES, s));
-  int32_t *d_levels = nullptr;
-  uint32_t *d_parents = nullptr;
-  if (levels) GG_TRY(ws(g, WS_MS_OUT0, (size_t)V * nroots, &d_levels));
-  if (parents) GG_TRY(ws(g, WS_MS_OUT1, (size_t)V * nroots, &d_parents));
-  ms_extract<<<grid_for(((size_t)V + 31) / 32, 1, g->num_sms, 16), 256, 0, s>>>(
-      V, nroots, b.visit, b.lvl, b.par, g->out.deg, d_levels, d_parents, b.lane_reached, b.lane_edges);
-  L.launches += 1;
-  GG_CUDA(cudaGetLastError());
-  GG_TRY(timed_end(g, stats, L.launches));
-  GG_TRY(tr.collect());
-  if (levels) GG_CUDA(cudaMemcpy(levels, d_levels, sizeof(int32_t) * V * nroots, cudaMemcpyDeviceToHost));
-  if (parents) GG_CUDA(cudaMemcpy(parents, d_parents, sizeof(uint32_t) * V * nroots, cudaMemcpyDeviceToHost));
-  u64 hr[2 * LANES];
-  GG_CUDA(cudaMemcpy(hr, b.lane_reached, sizeof(u64) * 2 * LANES, cudaMemcpyDeviceToHost));
-  if (reached) memcpy(reached, hr, sizeof(u64) * nroots);
-  if (lane_edges) memcpy(lane_edges, hr + LANES, sizeof(u64) * nroots);
-  g->result[0] = d_levels;
-  g->result[1] = d_parents;
-  return GG_OK;
 }
 
 // ---------------------------------------------------------------- batched SSSP
-namespace gg {
-
-__global__ void msp_roots(const uint32_t *roots, int n, u64 *front, float *dist, const uint32_t *out_deg,
-                          MsCounters *mc, uint32_t *q) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  u64 alive = 0, edges = 0;
-  unsigned nq = 0;
-  for (int l = 0; l < n; l++) {
-    uint32_t r = roots[l];
-    if (!front[r]) {
-      edges += out_deg[r];
-      if (out_deg[r]) q[nq++] = r;
-    }
-    front[r] |= 1ull << l;
-    dist[(size_t)r * LANES + l] = 0.0f;
-    alive |= 1ull << l;
-  }
-  mc->alive = alive;
-  mc->edges = edges;
-  mc->qlen = nq;
-}
 
 // Relaxation of every out-edge (u, v, w) of the union frontier, one warp per
 // edge: lane j handles SSSP lanes j and j + 32 of the edge (a coalesced 256 B
@@ -583,41 +457,313 @@ __global__ void __launch_bounds__(PUSH_THREADS)
   ms_flush(mc, t_alive, t_edges, 0);
 }
 
-// dist, lane-major, and per-lane reached counts (distance < 1e9).
-__global__ void __launch_bounds__(256)
-    msp_extract(uint32_t V, int n, const float *__restrict__ dist, float *out, u64 *reached) {
-  __shared__ float s_d[32][LANES + 1];
-  __shared__ u64 s_reach[LANES];
-  if (threadIdx.x < LANES) s_reach[threadIdx.x] = 0;
-  __syncthreads();
-  for (size_t v0 = (size_t)blockIdx.x * 32; v0 < V; v0 += (size_t)gridDim.x * 32) {
-    for (int i = threadIdx.x; i < 32 * LANES; i += blockDim.x) {
-      const int r = i / LANES, l = i % LANES;
-      if (v0 + r < V) s_d[r][l] = dist[(v0 + r) * LANES + l];
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 32 * n; i += blockDim.x) {
-      const int l = i / 32, r = i % 32;
-      const size_t v = v0 + r;
-      if (v >= V) continue;
-      const float x = s_d[r][l];
-      if (out) out[(size_t)l * V + v] = x;
-      if (x < 1e9f) atomicAdd(&s_reach[l], 1ull);
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x < (unsigned)n && s_reach[threadIdx.x]) atomicAdd(&reached[threadIdx.x], s_reach[threadIdx.x]);
-}
-
 }  // namespace gg
 
-extern "C" int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, float *distances, uint64_t *reached,
-                               gg_run_stats *stats) {
+// ---------------------------------------------------------------- LanePool
+namespace gg {
+
+size_t LanePool::bytes_needed(const gg_graph *g, Kind kind, bool parents) {
+  const size_t V = g->V;
+  size_t b = 3 * V * sizeof(u64) + 2 * (V + 1) * sizeof(uint32_t);            // masks, queues
+  b += (V + 2) * sizeof(u64) + scan_scratch_elems(V + 1) * sizeof(u64);       // degree prefix + scan
+  b += (bitmap_words32(g->V) + V + 1) * sizeof(uint32_t) + scan_scratch_elems(V) * sizeof(uint32_t);
+  if (kind == BFS) b += V * LANES * sizeof(uint32_t) * (parents ? 2 : 1);
+  else b += V * LANES * sizeof(float);
+  return b + (1 << 20);
+}
+
+int LanePool::open() {
+  if (open_) return GG_OK;
+  GG_CUDA(cudaSetDevice(g_->device));
+  const size_t V = g_->V;
+  auto fail = [&](cudaError_t e) {
+    close();
+    return cuda_status(e, "lane pool buffers");
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&front_, V * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMalloc(&next_, V * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMalloc(&q_[0], (V + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&q_[1], (V + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&prefix_, (V + 2) * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMalloc(&scan64_, scan_scratch_elems(V + 1) * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMalloc(&qpos_, (V + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&scan32_, scan_scratch_elems(V) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&roots_dev_, LANES * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&start_dev_, LANES * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&lanes_dev_, LANES * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&mc_, 256);
+  if (e == cudaSuccess) e = cudaMallocHost(&mc_host_, 256);
+  if (e == cudaSuccess) e = cudaMalloc(&out_dev_, 3 * LANES * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMallocHost(&out_host_, 3 * LANES * sizeof(u64));
+  if (kind_ == BFS) {
+    if (e == cudaSuccess) e = cudaMalloc(&visit_, V * sizeof(u64));
+    if (e == cudaSuccess) e = cudaMalloc(&lvl_, V * LANES * sizeof(uint32_t));
+    if (e == cudaSuccess && parents_) e = cudaMalloc(&par_, V * LANES * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(visit_, 0, V * sizeof(u64), s_);
+  } else {
+    if (e == cudaSuccess) e = cudaMalloc(&dist_, V * LANES * sizeof(float));
+    if (e == cudaSuccess) {
+      fill_kernel<float><<<grid_for(V * LANES, 256, g_->num_sms, 16), 256, 0, s_>>>(dist_, V * LANES, 1e9f);
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(front_, 0, V * sizeof(u64), s_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+  if (e != cudaSuccess) return fail(e);
+  used_ = active_ = 0;
+  ae_ = 0;
+  nq_ = 0;
+  qvalid_ = true;
+  next_clear_ = false;
+  cur_ = 0;
+  iter_ = 0;
+  open_ = true;
+  return GG_OK;
+}
+
+void LanePool::close() {
+  if (s_) cudaStreamSynchronize(s_);
+  void *bufs[] = {visit_, front_, next_, lvl_, par_, dist_, q_[0], q_[1], prefix_, scan64_, qpos_, scan32_,
+                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_};
+  for (void *p : bufs)
+    if (p) cudaFree(p);
+  if (mc_host_) cudaFreeHost(mc_host_);
+  if (out_host_) cudaFreeHost(out_host_);
+  if (s_) cudaStreamDestroy(s_);
+  visit_ = front_ = next_ = nullptr;
+  lvl_ = par_ = nullptr;
+  dist_ = nullptr;
+  q_[0] = q_[1] = nullptr;
+  prefix_ = scan64_ = nullptr;
+  qpos_ = scan32_ = roots_dev_ = start_dev_ = nullptr;
+  lanes_dev_ = nullptr;
+  mc_ = mc_host_ = nullptr;
+  out_dev_ = out_host_ = nullptr;
+  s_ = nullptr;
+  open_ = false;
+}
+
+int LanePool::read_counters(LaneCounters *h) {
+  GG_CUDA(cudaMemcpyAsync(mc_host_, mc_, sizeof(LaneCounters), cudaMemcpyDeviceToHost, s_));
+  GG_CUDA(cudaStreamSynchronize(s_));
+  *h = *mc_host_;
+  return GG_OK;
+}
+
+int LanePool::admit(const uint32_t *roots, const int *lanes, int n) {
+  if (n <= 0) return GG_OK;
+  u64 mask = 0;
+  for (int i = 0; i < n; i++) {
+    if (lanes[i] < 0 || lanes[i] >= LANES || ((used_ >> lanes[i]) & 1ull) || roots[i] >= g_->V) {
+      set_error("bad lane or root in admit");
+      return GG_ERR_INVALID;
+    }
+    mask |= 1ull << lanes[i];
+    start_[lanes[i]] = iter_;
+  }
+  const uint32_t V = g_->V;
+  GG_CUDA(cudaMemcpyAsync(roots_dev_, roots, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s_));
+  GG_CUDA(cudaMemcpyAsync(lanes_dev_, lanes, sizeof(int) * n, cudaMemcpyHostToDevice, s_));
+  GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
+  if (kind_ == BFS)
+    lanes_reset_visit<<<grid_for(V, 256, g_->num_sms, 8), 256, 0, s_>>>(visit_, V, mask);
+  else
+    lanes_reset_dist<<<grid_for((size_t)V * LANES, 256, g_->num_sms, 16), 256, 0, s_>>>(dist_, V, mask);
+  GG_CUDA(cudaMemsetAsync(mc_, 0, sizeof(LaneCounters), s_));
+  lanes_admit<<<1, 32, 0, s_>>>(roots_dev_, lanes_dev_, n, front_, visit_, lvl_, par_, dist_, iter_, g_->out.deg, mc_);
+  launches += 2;
+  GG_CUDA(cudaGetLastError());
+  LaneCounters h;
+  GG_TRY(read_counters(&h));
+  ae_ += h.edges;
+  qvalid_ = false;
+  used_ |= mask;
+  active_ |= mask;
+  return GG_OK;
+}
+
+int LanePool::build_queue() {
+  const uint32_t V = g_->V;
+  GG_CUDA((exclusive_scan<uint32_t, NonzeroMask>(NonzeroMask{front_}, V, qpos_, scan32_, s_, &launches)));
+  ms_compact<<<grid_for(V, 256, g_->num_sms), 256, 0, s_>>>(front_, V, qpos_, q_[cur_]);
+  launches += 1;
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(mc_host_, qpos_ + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, s_));
+  GG_CUDA(cudaStreamSynchronize(s_));
+  nq_ = *(uint32_t *)mc_host_;
+  qvalid_ = true;
+  return GG_OK;
+}
+
+static unsigned push_grid_for(const gg_graph *g, unsigned long long total) {
+  unsigned long long tiles = (total + PUSH_TILE - 1) / PUSH_TILE;
+  unsigned long long cap = (unsigned long long)g->num_sms * 8;
+  return (unsigned)(tiles < 1 ? 1 : (tiles > cap ? cap : tiles));
+}
+
+int LanePool::bfs_step() {
+  const uint32_t V = g_->V;
+  const bool sparse = ae_ < g_->E / 20;
+  if (tr_) tr_->add(sparse ? 0 : 1, ae_, 0);
+  iter_ += 1;
+  LaneCounters h;
+  GG_CUDA(cudaMemsetAsync(mc_, 0, sizeof(LaneCounters), s_));
+  if (sparse) {
+    if (!qvalid_) GG_TRY(build_queue());
+    if (!next_clear_) GG_CUDA(cudaMemsetAsync(next_, 0, sizeof(u64) * V, s_));
+    if (ae_ > 0) {
+      GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
+                                                                 scan64_, s_, &launches)));
+      if (tr_) GG_TRY(tr_->kbegin());
+      ms_push<<<push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, visit_,
+                                                               next_, lvl_, par_, iter_, q_[cur_ ^ 1], mc_);
+      if (tr_) GG_TRY(tr_->kend());
+      launches += 1;
+    }
+    LaneCounters hq;
+    GG_TRY(read_counters(&hq));
+    if (hq.qlen)
+      ms_push_finish<<<grid_for(hq.qlen, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_ ^ 1], hq.qlen, visit_, next_,
+                                                                        g_->out.deg, mc_);
+    ms_clear_queue<<<grid_for(nq_ ? nq_ : 1, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
+    launches += 2;
+    GG_TRY(read_counters(&h));
+    nq_ = h.qlen;
+    qvalid_ = true;
+    cur_ ^= 1;
+    next_clear_ = true;
+  } else {
+    if (tr_) GG_TRY(tr_->kbegin());
+    ms_pull_light<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+        g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_, g_->out.deg, mc_);
+    launches += 1;
+    if (g_->in.nbig) {
+      ms_pull_chunks<<<grid_for((size_t)g_->in.nbigchunks * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+          g_->in, active_, front_, visit_, next_, lvl_, par_, iter_);
+      ms_big_finish<<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_);
+      launches += 2;
+    }
+    if (tr_) GG_TRY(tr_->kend());
+    GG_TRY(read_counters(&h));
+    qvalid_ = false;
+    next_clear_ = false;
+  }
+  GG_CUDA(cudaGetLastError());
+  if (tr_) tr_->set_activated(h.touched);
+  active_ &= h.alive;
+  ae_ = h.edges;
+  u64 *t = front_;
+  front_ = next_;
+  next_ = t;
+  return GG_OK;
+}
+
+int LanePool::sssp_step() {
+  if (tr_) tr_->add(0, ae_, 0);
+  iter_ += 1;
+  if (!qvalid_) GG_TRY(build_queue());
+  GG_CUDA(cudaMemsetAsync(mc_, 0, sizeof(LaneCounters), s_));
+  if (!next_clear_) GG_CUDA(cudaMemsetAsync(next_, 0, sizeof(u64) * g_->V, s_));
+  if (ae_ > 0 && nq_ > 0) {
+    GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
+                                                               scan64_, s_, &launches)));
+    if (tr_) GG_TRY(tr_->kbegin());
+    msp_push<<<push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
+                                                              dist_, q_[cur_ ^ 1], mc_);
+    if (tr_) GG_TRY(tr_->kend());
+    launches += 1;
+  }
+  ms_clear_queue<<<grid_for(nq_ ? nq_ : 1, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
+  launches += 1;
+  GG_CUDA(cudaGetLastError());
+  LaneCounters h;
+  GG_TRY(read_counters(&h));
+  if (tr_) tr_->set_activated(h.qlen);
+  nq_ = h.qlen;
+  qvalid_ = true;
+  next_clear_ = true;
+  cur_ ^= 1;
+  active_ &= h.alive;
+  ae_ = h.edges;
+  u64 *t = front_;
+  front_ = next_;
+  next_ = t;
+  return GG_OK;
+}
+
+int LanePool::step() {
+  if (!active_) return GG_OK;
+  calls_ += 1;
+  return kind_ == BFS ? bfs_step() : sssp_step();
+}
+
+int LanePool::digest(u64 mask, u64 *reached, u64 *checksum, u64 *edges) {
+  mask &= used_;
+  if (!mask) return GG_OK;
+  const uint32_t V = g_->V;
+  GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
+  GG_CUDA(cudaMemsetAsync(out_dev_, 0, 3 * LANES * sizeof(u64), s_));
+  lanes_digest<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+      V, mask, kind_ == BFS ? visit_ : nullptr, lvl_, start_dev_, dist_, g_->out.deg, out_dev_);
+  launches += 1;
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(out_host_, out_dev_, 3 * LANES * sizeof(u64), cudaMemcpyDeviceToHost, s_));
+  GG_CUDA(cudaStreamSynchronize(s_));
+  for (int l = 0; l < LANES; l++) {
+    if (!((mask >> l) & 1ull)) continue;
+    if (reached) reached[l] = out_host_[l];
+    if (checksum) checksum[l] = out_host_[LANES + l];
+    if (edges) edges[l] = out_host_[2 * LANES + l];
+  }
+  return GG_OK;
+}
+
+int LanePool::extract(u64 mask, int32_t *levels, uint32_t *parents, float *dist) {
+  mask &= used_;
+  int lanes[LANES], n = 0;
+  for (int l = 0; l < LANES; l++)
+    if ((mask >> l) & 1ull) lanes[n++] = l;
+  if (!n) return GG_OK;
+  const uint32_t V = g_->V;
+  GG_CUDA(cudaMemcpyAsync(lanes_dev_, lanes, sizeof(int) * n, cudaMemcpyHostToDevice, s_));
+  GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
+  lanes_extract<<<grid_for(((size_t)V + 31) / 32, 1, g_->num_sms, 16), 256, 0, s_>>>(
+      V, lanes_dev_, n, visit_, lvl_, start_dev_, par_, dist_, kind_ == BFS ? levels : nullptr,
+      kind_ == BFS ? parents : nullptr, kind_ == SSSP ? dist : nullptr);
+  launches += 1;
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaStreamSynchronize(s_));
+  return GG_OK;
+}
+
+// The graph's own pools for the batched calls (created on first use).
+static LanePool *graph_pool(gg_graph *g, LanePool::Kind kind, bool parents, int *status) {
+  LanePool *&p = kind == LanePool::BFS ? g->pool_bfs : g->pool_sssp;
+  if (p && kind == LanePool::BFS && parents && !p->parents()) {
+    delete p;
+    p = nullptr;
+  }
+  if (!p) p = new LanePool(g, kind, parents);
+  *status = p->open();
+  return p;
+}
+
+void pools_destroy(gg_graph *g) {
+  delete g->pool_bfs;
+  delete g->pool_sssp;
+  g->pool_bfs = g->pool_sssp = nullptr;
+}
+
+// Runs one batch of roots to completion on the graph's pool.
+static int run_batch(gg_graph *g, LanePool::Kind kind, const uint32_t *roots, int nroots, bool parents,
+                     int32_t *levels, uint32_t *par_out, float *dist_out, uint64_t *reached, uint64_t *checksum,
+                     uint64_t *lane_edges, gg_run_stats *stats) {
   if (!g || !roots || nroots < 1 || nroots > LANES) {
     set_error("need a graph and 1..64 roots");
     return GG_ERR_INVALID;
   }
-  if (!g->weighted) {
+  if (kind == LanePool::SSSP && !g->weighted) {
     set_error("sssp needs a weighted graph");
     return GG_ERR_UNWEIGHTED;
   }
@@ -627,69 +773,79 @@ extern "C" int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, f
       return GG_ERR_INVALID;
     }
   GG_CUDA(cudaSetDevice(g->device));
-  const uint32_t V = g->V;
-  u64 *front, *next;
-  float *dist;
-  uint32_t *q[2], *d_roots;
-  char *blob;
-  GG_TRY(ws(g, WS_MS_FRONT, V, &front));
-  GG_TRY(ws(g, WS_MS_NEXT, V, &next));
-  GG_TRY(ws(g, WS_MS_DIST, (size_t)V * LANES, &dist));
-  GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
-  GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
-  GG_TRY(ws(g, WS_MS_ROOTS, LANES, &d_roots));
-  GG_TRY(ws(g, WS_MS_MISC, 256 + sizeof(u64) * 2 * LANES, &blob));
-  MsCounters *mc = (MsCounters *)blob;
-  u64 *lane_reached = (u64 *)(blob + 256);
-  Launch L(g);
+  int status = GG_OK;
+  LanePool *p = graph_pool(g, kind, parents, &status);
+  if (status != GG_OK) return status;
   Trace tr(stats, g);
-  cudaStream_t s = g->stream;
-  GG_TRY(timed_begin(g));
-  GG_CUDA(cudaMemcpyAsync(d_roots, roots, sizeof(uint32_t) * nroots, cudaMemcpyHostToDevice, s));
-  GG_CUDA(cudaMemsetAsync(front, 0, sizeof(u64) * V, s));
-  GG_CUDA(cudaMemsetAsync(next, 0, sizeof(u64) * V, s));
-  GG_CUDA(cudaMemsetAsync(blob, 0, 256 + sizeof(u64) * 2 * LANES, s));
-  fill_kernel<float><<<grid_for((size_t)V * LANES, 256, g->num_sms, 16), 256, 0, s>>>(dist, (size_t)V * LANES, 1e9f);
-  msp_roots<<<1, 32, 0, s>>>(d_roots, nroots, front, dist, g->out.deg, mc, q[0]);
-  L.launches += 2;
-  GG_CUDA(cudaGetLastError());
-  MsCounters h;
-  GG_TRY(ms_read(g, mc, &h));
-  uint32_t nq = h.qlen;
-  unsigned long long ae = h.edges;
-  int cur = 0;
-  while (nq > 0 && ae > 0) {
-    tr.add(0, ae, 0);
-    GG_CUDA(cudaMemsetAsync(mc, 0, sizeof(MsCounters), s));
-    unsigned long long *P;
-    GG_TRY(L.scan_queue_degrees(q[cur], nq, g->out.deg, &P));
-    GG_TRY(tr.kbegin());
-    msp_push<<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[cur], P, nq, ae, g->out, front, next, dist, q[cur ^ 1], mc);
-    GG_TRY(tr.kend());
-    // the old frontier becomes next: clear its entries
-    ms_clear_queue<<<grid_for(nq, 256, g->num_sms), 256, 0, s>>>(q[cur], nq, front);
-    L.launches += 2;
-    GG_CUDA(cudaGetLastError());
-    GG_TRY(ms_read(g, mc, &h));
-    tr.set_activated(h.qlen);
-    nq = h.qlen;
-    ae = h.edges;
-    u64 *t = front;
-    front = next;
-    next = t;
-    cur ^= 1;
+  p->set_trace(&tr);
+  p->launches = 0;
+  const uint32_t V = g->V;
+  int lanes[LANES];
+  for (int i = 0; i < nroots; i++) lanes[i] = i;
+  cudaStream_t gs = g->stream;
+  g->stream = p->stream();  // events and traces on the pool's stream
+  status = timed_begin(g);
+  if (status == GG_OK) status = p->admit(roots, lanes, nroots);
+  while (status == GG_OK && p->active()) status = p->step();
+  const u64 mask = nroots == 64 ? ~0ull : ((1ull << nroots) - 1);
+  u64 r[LANES], c[LANES], e[LANES];
+  if (status == GG_OK) status = p->digest(mask, r, c, e);
+  int32_t *d_lv = nullptr;
+  uint32_t *d_pa = nullptr;
+  float *d_di = nullptr;
+  if (status == GG_OK && levels) status = ws(g, WS_MS_OUT0, (size_t)V * nroots, &d_lv);
+  if (status == GG_OK && par_out) status = ws(g, WS_MS_OUT1, (size_t)V * nroots, &d_pa);
+  if (status == GG_OK && dist_out) status = ws(g, WS_MS_OUT0, (size_t)V * nroots, &d_di);
+  if (status == GG_OK && (d_lv || d_pa || d_di)) status = p->extract(mask, d_lv, d_pa, d_di);
+  if (status == GG_OK) status = timed_end(g, stats, p->launches);
+  if (status == GG_OK) status = tr.collect();
+  g->stream = gs;
+  p->retire(mask);
+  p->set_trace(nullptr);
+  if (status != GG_OK) return status;
+  if (levels) GG_CUDA(cudaMemcpy(levels, d_lv, sizeof(int32_t) * V * nroots, cudaMemcpyDeviceToHost));
+  if (par_out) GG_CUDA(cudaMemcpy(par_out, d_pa, sizeof(uint32_t) * V * nroots, cudaMemcpyDeviceToHost));
+  if (dist_out) GG_CUDA(cudaMemcpy(dist_out, d_di, sizeof(float) * V * nroots, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < nroots; i++) {
+    if (reached) reached[i] = r[i];
+    if (checksum) checksum[i] = c[i];
+    if (lane_edges) lane_edges[i] = e[i];
   }
-  float *d_out = nullptr;
-  if (distances) GG_TRY(ws(g, WS_MS_OUT0, (size_t)V * nroots, &d_out));
-  GG_CUDA(cudaMemsetAsync(lane_reached, 0, sizeof(u64) * LANES, s));
-  msp_extract<<<grid_for(((size_t)V + 31) / 32, 1, g->num_sms, 16), 256, 0, s>>>(V, nroots, dist, d_out, lane_reached);
-  L.launches += 1;
-  GG_CUDA(cudaGetLastError());
-  GG_TRY(timed_end(g, stats, L.launches));
-  GG_TRY(tr.collect());
-  if (distances) GG_CUDA(cudaMemcpy(distances, d_out, sizeof(float) * V * nroots, cudaMemcpyDeviceToHost));
-  if (reached) GG_CUDA(cudaMemcpy(reached, lane_reached, sizeof(u64) * nroots, cudaMemcpyDeviceToHost));
-  g->result[0] = d_out;
-  g->result[1] = nullptr;
+  g->result[0] = d_lv ? (const void *)d_lv : (const void *)d_di;
+  g->result[1] = d_pa;
   return GG_OK;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" int gg_bfs_batched(gg_graph *g, const uint32_t *roots, int nroots, int32_t *levels, uint32_t *parents,
+                              uint64_t *reached, uint64_t *lane_edges, gg_run_stats *stats) {
+  return run_batch(g, LanePool::BFS, roots, nroots, parents != nullptr, levels, parents, nullptr, reached, nullptr,
+                   lane_edges, stats);
+}
+
+extern "C" int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, float *distances, uint64_t *reached,
+                               gg_run_stats *stats) {
+  return run_batch(g, LanePool::SSSP, roots, nroots, false, nullptr, nullptr, distances, reached, nullptr, nullptr,
+                   stats);
+}
+
+extern "C" uint64_t gg_result_checksum(const void *values, uint32_t vertices, int kind) {
+  uint64_t sum = 0;
+  for (uint32_t v = 0; v < vertices; v++) {
+    uint32_t x;
+    if (kind == 0) {
+      int32_t lv = ((const int32_t *)values)[v];
+      if (lv < 0) continue;
+      x = (uint32_t)lv;
+    } else {
+      float d = ((const float *)values)[v];
+      if (!(d < 1e9f)) continue;
+      memcpy(&x, &d, 4);
+    }
+    sum += gg_mix64((uint64_t)v * 0x9E3779B97F4A7C15ull + x);
+  }
+  return sum;
 }

@@ -113,6 +113,9 @@ struct Workspace {
   Counters *ctr_host = nullptr;  // pinned mirror
 };
 
+class LanePool;
+void pools_destroy(gg_graph *g);
+
 }  // namespace gg
 
 struct gg_graph {
@@ -129,6 +132,8 @@ struct gg_graph {
   int num_sms = 0;
   const void *result[2] = {nullptr, nullptr};
   std::vector<cudaEvent_t> evpool;  // events for per-call kernel timing
+  gg::LanePool *pool_bfs = nullptr;  // lane pools of the batched calls
+  gg::LanePool *pool_sssp = nullptr;
 };
 
 namespace gg {

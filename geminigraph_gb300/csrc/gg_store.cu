@@ -488,6 +488,7 @@ void graph_destroy(gg_graph *g) {
   if (!g) return;
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
+  pools_destroy(g);
   bool alias = g->in.nbr == g->out.nbr;
   free_dir(&g->out);
   if (!alias) free_dir(&g->in);

@@ -156,6 +156,58 @@ int gg_bfs_batched(gg_graph *g, const uint32_t *roots, int nroots, int32_t *leve
 int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, float *distances, uint64_t *reached,
                     gg_run_stats *stats);
 
+/* Checksum of one traversal result, as the serving loop reports it: the sum
+ * (mod 2^64) over reached vertices v of mix64(v * 0x9E3779B97F4A7C15 + x), where
+ * x is the hop count (kind 0: int32 levels, -1 = unreached) or the float bits
+ * of the distance (kind 1: float distances, >= 1e9 = unreached) and mix64 is
+ * the SplitMix64 finaliser. */
+uint64_t gg_result_checksum(const void *values, uint32_t vertices, int kind);
+
+/* Hop count of every vertex in a BFS parent array (-1 if unreached); host code. */
+int gg_levels_from_parents(const uint32_t *parent, uint32_t vertices, uint32_t root, int32_t *levels);
+
+/* ---- serving loop (no counterpart in the reference) ----
+ * Resident graphs answer BFS (kind 0) and SSSP (kind 1) queries with
+ * continuous batching: every (graph, kind) has a pool of 64 lanes on its own
+ * stream and worker thread; queries join free lanes between iterations and
+ * leave when their traversal ends, so queries of different graphs and kinds
+ * overlap on the device.  A pool is opened only if its buffers fit the budget
+ * and the device's free memory; its queries wait otherwise.  Each result
+ * carries the query's reached count and gg_result_checksum of its result
+ * array, identical to a single-root gg_bfs / gg_sssp run of the same root. */
+typedef struct gg_server gg_server;
+
+typedef struct {
+  uint64_t ticket;
+  int32_t graph;
+  int32_t kind;
+  uint32_t root;
+  int32_t status;
+  uint64_t reached;
+  uint64_t checksum;
+  uint64_t active_edges;     /* BFS: the single-root TEPS numerator */
+  double latency_ms;         /* submit to completion, host clock */
+} gg_query_result;
+
+typedef struct {
+  uint64_t completed, pending, pools_open, pools_opened, pools_closed, admission_waits;
+  uint64_t bytes_in_use, budget;
+  int32_t max_busy_pools;    /* most pools running at once */
+  int32_t max_lanes_in_use;  /* most queries on the device at once */
+} gg_server_stats;
+
+/* Device bytes one pool of kind (0 BFS, 1 SSSP) on g holds while open. */
+uint64_t gg_pool_bytes(const gg_graph *g, int kind);
+/* hbm_budget: device bytes the pools may hold (0 = free memory less 2 GiB). */
+int gg_server_create(int device, uint64_t hbm_budget, gg_server **out);
+/* The graph must outlive the server; calls on it must not overlap serving. */
+int gg_server_add_graph(gg_server *s, gg_graph *g, int *graph_id);
+int gg_server_submit(gg_server *s, int graph_id, int kind, uint32_t root, uint64_t *ticket);
+/* Up to max_results completed queries; waits up to timeout_ms for the first. */
+int gg_server_wait(gg_server *s, gg_query_result *out, int max_results, int timeout_ms, int *n);
+int gg_server_stats_get(gg_server *s, gg_server_stats *stats);
+int gg_server_free(gg_server *s);
+
 /* Device address of the last result of a toolkit kept on the device:
  * which = 0 primary output (parent / ranks / label / distance / dependencies),
  * 1 secondary (inv_num_paths).  Valid until the next toolkit call on g. */

@@ -59,12 +59,16 @@ WORKLOADS = {
                      desc="BFS on the 8192 x 8192 4-neighbour grid (both directions)"),
     "bfs_batched": dict(kind="rmat", scale=24, ef=16, weighted=False, symmetric=False,
                         desc="batched BFS, 64 seeded roots per launch, on directed R-MAT scale 24, edge factor 16"),
+    "serve": dict(kind="rmat", scale=26, ef=16, weighted=True, symmetric=False,
+                  desc="serving: 4 resident weighted R-MAT graphs (scales 20, 22, 24, 26, edge factor 16), Poisson "
+                       "arrivals at 5000 queries/s, graph drawn with p = 0.4/0.3/0.2/0.1, 75% BFS / 25% SSSP, "
+                       "seeded uniform non-isolated roots"),
     "sssp_batched": dict(kind="rmat", scale=24, ef=16, weighted=True, symmetric=False,
                          desc="batched SSSP, 64 seeded roots per launch, on R-MAT scale 24, edge factor 16, "
                               "float weights in [0,1)"),
 }
 REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs",
-           "bfs_batched": "bfs", "sssp_batched": "sssp"}
+           "bfs_batched": "bfs", "sssp_batched": "sssp", "serve": "bfs"}
 
 
 def log(*a):
@@ -235,7 +239,7 @@ def step_args(gg, g, workload, count):
 # ----------------------------------------------------------------- CPU side
 def ref_sample_scale(workload):
     return {"bfs": 22, "cc": 21, "pagerank": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024, "bfs_batched": 22,
-            "sssp_batched": 21}[workload]
+            "sssp_batched": 21, "serve": 22}[workload]
 
 
 def cpu_reference(gg, workload, nsteps, warmup):
@@ -257,7 +261,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
     src, dst = words[:, 0].copy(), words[:, 1].copy()
     wts = words[:, 2].view(np.float32).copy() if w["weighted"] else None
     n = warmup + nsteps
-    if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched"):
+    if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched", "serve"):
         args = gg.pick_roots(np.bincount(src, minlength=V), n, seed=SEED + 2000)
     elif workload == "bfs_grid":
         args = [0] * n
@@ -269,7 +273,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
     og = OracleGraph(V, src, dst, wts, symmetric=w["symmetric"])
     numer = []
     for a in args:
-        if workload in ("bfs", "bfs_grid", "bfs_batched"):
+        if workload in ("bfs", "bfs_grid", "bfs_batched", "serve"):
             tr = og.bfs(a)[1]
         elif workload in ("sssp", "sssp_batched"):
             tr = og.sssp(a)[1]
@@ -304,7 +308,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
     t, e = [], []
     for i, a in enumerate(args):
         t0 = time.perf_counter()
-        if workload in ("bfs", "bfs_grid", "bfs_batched"):
+        if workload in ("bfs", "bfs_grid", "bfs_batched", "serve"):
             og.bfs(a)
         elif workload in ("sssp", "sssp_batched"):
             og.sssp(a)
@@ -526,6 +530,117 @@ def gpu_arm_batched(args, dist):
     return 0
 
 
+def pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(round(q / 100.0 * (len(xs) - 1))))] if xs else None
+
+
+def gpu_arm_serve(args, dist):
+    """One step = one query of the stream.  value = completed queries / the
+    span from the first arrival to the last completion; plain = the first
+    args.plain queries run one at a time through gg_bfs / gg_sssp with the same
+    arrival times (FIFO, device time as service time)."""
+    import threading
+
+    import geminigraph_gb300 as gg
+    device = dist.local_rank
+    rng = np.random.default_rng(SEED + 77)
+    scales, probs = (20, 22, 24, 26), (0.4, 0.3, 0.2, 0.1)
+    t0 = time.perf_counter()
+    graphs = [gg.Graph.generate(gg.RMAT, sc, 16, SEED + i, weighted=True, device=device) for i, sc in enumerate(scales)]
+    build_s = time.perf_counter() - t0
+    degs = [g.out_degree() for g in graphs]
+    n = args.queries
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    gsel = rng.choice(len(scales), size=n, p=probs)
+    kinds = (rng.random(n) < 0.25).astype(int)
+    roots = [gg.pick_roots(degs[j], 1, int(rng.integers(1 << 30)))[0] for j in gsel]
+    queries = list(zip(gsel.tolist(), kinds.tolist(), roots))
+    # warm-up: one batch per (graph, kind) opens the pools' code paths
+    server = gg.Server(device=device)
+    ids = [server.add_graph(g) for g in graphs]
+    for j in range(len(graphs)):
+        for k in (0, 1):
+            server.submit(ids[j], k, gg.pick_roots(degs[j], 1, 5)[0])
+    got = 0
+    while got < 2 * len(graphs):
+        got += len(server.wait(timeout_ms=1000))
+    clocks = ClockSampler(device)
+    clocks.start()
+    results = {}
+    tickets = {}
+
+    def client():
+        start = time.perf_counter()
+        for i, (j, k, r) in enumerate(queries):
+            due = start + arrivals[i]
+            while True:
+                now = time.perf_counter()
+                if now >= due:
+                    break
+                time.sleep(min(due - now, 0.0005))
+            tickets[server.submit(ids[j], k, r)] = i
+
+    wall0 = time.perf_counter()
+    th = threading.Thread(target=client)
+    th.start()
+    while len(results) < n:
+        for r in server.wait(max_results=1024, timeout_ms=50):
+            results[r["ticket"]] = r
+        if not th.is_alive() and len(results) >= n:
+            break
+    th.join()
+    span = time.perf_counter() - wall0
+    clk = clocks.stop()
+    st = server.stats()
+    served = {tickets[t]: r for t, r in results.items()}
+    lat = [served[i]["latency_ms"] for i in range(n)]
+    # plain: the first args.plain queries one at a time, FIFO on the same arrivals
+    m = min(args.plain, n)
+    done_t, plain_lat, mism = 0.0, [], 0
+    for i in range(m):
+        j, k, r = queries[i]
+        g = graphs[j]
+        if k == 0:
+            parent, s1 = g.bfs(r)
+            chk = gg.result_checksum(gg.levels_from_parents(parent, r), 0)
+        else:
+            d1, s1 = g.sssp(r)
+            chk = gg.result_checksum(d1, 1)
+        svc = s1.device_ms / 1000.0
+        begin = max(arrivals[i], done_t)
+        done_t = begin + svc
+        plain_lat.append((done_t - arrivals[i]) * 1000.0)
+        mism += int(chk != served[i]["checksum"])
+    plain_qps = m / (done_t - arrivals[0]) if m else None
+    value = n / span
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": args.gpus, "steps": n,
+        "warmup": 2 * len(graphs), "ms_per_step": round(span * 1000 / n, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 lane masks / f32",
+        "data": "synthetic (seeded R-MAT generated on the device; Poisson query stream)",
+        "config": {"workload": WORKLOADS["serve"]["desc"], "queries": n, "rate_qps": args.rate,
+                   "graph_build_s": round(build_s, 2), "parallelism": f"replicas x{args.gpus}"},
+        "latency_ms": {"p50": round(pct(lat, 50), 3), "p99": round(pct(lat, 99), 3)},
+        "plain": {"value": round(plain_qps, 1) if plain_qps else None, "unit": "queries/s",
+                  "latency_ms": {"p50": round(pct(plain_lat, 50), 3), "p99": round(pct(plain_lat, 99), 3)},
+                  "what": f"first {m} queries one at a time through gg_bfs / gg_sssp, FIFO on the same arrivals"},
+        "speedup_vs_plain": round(value / plain_qps, 2) if plain_qps else None,
+        "checksum_mismatches": mism, "checked": m,
+        "server": {k: st[k] for k in ("pools_opened", "pools_closed", "admission_waits", "max_busy_pools",
+                                      "max_lanes_in_use")},
+        "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 4,
+                "d2h_bytes_per_step": 16, "note": "per query the root in and reached count + checksum out"},
+        "clocks": clk,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    server.close()
+    for g in graphs:
+        g.close()
+    return 0
+
+
 def run_once_stats(gg, g, workload, a, st):
     L = gg.library()
     import ctypes
@@ -569,6 +684,9 @@ def main():
     ap.add_argument("--workload", default="bfs", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=int, default=None, help="override the workload's R-MAT scale / grid side")
+    ap.add_argument("--queries", type=int, default=2000, help="serve: queries in the stream")
+    ap.add_argument("--rate", type=float, default=5000.0, help="serve: mean arrival rate (queries/s)")
+    ap.add_argument("--plain", type=int, default=300, help="serve: queries replayed one at a time")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
@@ -584,6 +702,8 @@ def main():
             return reference_arm(args, dist)
         if args.workload.endswith("_batched"):
             return gpu_arm_batched(args, dist)
+        if args.workload == "serve":
+            return gpu_arm_serve(args, dist)
         return gpu_arm(args, dist)
     finally:
         dist.close()

@@ -63,8 +63,41 @@ def build_library(verbose=False):
     return LIB
 
 
+CPP = os.path.join(PKG, "cpp")
+BIN = os.path.join(PKG, "bin")
+TOOLKITS = ("bfs", "cc", "pagerank", "sssp", "bc")
+
+
+def build_toolkits(verbose=False):
+    """The five command lines (toolkits/*.cpp of the reference, same argv and
+    output) against libgemini_gb300.so, with g++."""
+    os.makedirs(BIN, exist_ok=True)
+    headers = glob.glob(os.path.join(CPP, "*", "*.hpp")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    jobs = []
+    for app in TOOLKITS:
+        src = os.path.join(CPP, "toolkits", app + ".cpp")
+        out = os.path.join(BIN, app)
+        if _stale(out, [src, LIB] + headers):
+            jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++11", "-I", INCLUDE, "-I", CPP,
+                         "-I", os.path.join(CPP, "toolkits"), src, "-o", out, "-L", PKG, "-lgemini_gb300",
+                         "-Wl,-rpath,$ORIGIN/..", "-lpthread"])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("g++ failed:\n" + " ".join(cmd) + "\n" + p.stdout + p.stderr)
+
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(run, jobs))
+    return BIN
+
+
 def build(verbose=False):
-    return build_library(verbose)
+    lib = build_library(verbose)
+    build_toolkits(verbose)
+    return lib
 
 
 if __name__ == "__main__":

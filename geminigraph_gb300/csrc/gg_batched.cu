@@ -410,6 +410,9 @@ __global__ void __launch_bounds__(PUSH_THREADS)
     msp_push(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
              unsigned long long total, Dir d, const u64 *__restrict__ front, u64 *next, float *dist, uint32_t *q_out,
              MsCounters *mc) {
+  __shared__ unsigned long long s_P[PUSH_STAGE + 1];
+  __shared__ unsigned long long s_base[PUSH_STAGE];
+  __shared__ uint32_t s_src[PUSH_STAGE];
   __shared__ uint32_t s_lo, s_hi;
   const unsigned lane = lane_id(), w = threadIdx.x >> 5;
   const unsigned long long ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
@@ -423,12 +426,31 @@ __global__ void __launch_bounds__(PUSH_THREADS)
       s_hi = upper_bound_idx<unsigned long long>(P, lo, n + 1, e1 - 1);
     }
     __syncthreads();
-    const uint32_t lo = s_lo, hi = s_hi;
+    const uint32_t lo = s_lo, hi = s_hi, cnt = hi - lo;
+    const bool staged = cnt <= (uint32_t)PUSH_STAGE;
+    if (staged) {
+      for (uint32_t i = threadIdx.x; i < cnt; i += PUSH_THREADS) {
+        const unsigned long long pi = P[lo + i];
+        const uint32_t src = q[lo + i];
+        s_P[i] = pi;
+        s_src[i] = src;
+        s_base[i] = d.off[src] - pi;
+      }
+    }
     __syncthreads();
+    // each warp takes every eighth edge of the tile; its lanes cover the 64 SSSP lanes
     for (unsigned long long e = e0 + w; e < e1; e += PUSH_THREADS / 32) {
-      const uint32_t i = upper_bound_idx<unsigned long long>(P, lo, hi, e) - 1;
-      const uint32_t u = q[i];
-      const unsigned long long k = d.off[u] + (e - P[i]);
+      uint32_t u;
+      unsigned long long k;
+      if (staged) {
+        const uint32_t i = upper_bound_idx<unsigned long long>(s_P, 0, cnt, e) - 1;
+        u = s_src[i];
+        k = s_base[i] + e;
+      } else {
+        const uint32_t i = upper_bound_idx<unsigned long long>(P, lo, hi, e) - 1;
+        u = q[i];
+        k = d.off[u] + (e - P[i]);
+      }
       const uint32_t v = d.nbr[k];
       const float wt = d.w[k];
       const u64 fm = front[u];
@@ -453,6 +475,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
         t_alive |= low;
       }
     }
+    __syncthreads();
   }
   ms_flush(mc, t_alive, t_edges, 0);
 }

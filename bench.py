@@ -50,7 +50,10 @@ WORKLOADS = {
     "cc": dict(kind="rmat", scale=26, ef=16, weighted=False, symmetric=True,
                desc="CC (min-label, symmetrised edges) on R-MAT scale 26, edge factor 16"),
     "pagerank": dict(kind="rmat", scale=20, ef=16, weighted=False, symmetric=False,
-                     desc="PageRank 20 iterations (double) on directed R-MAT scale 20, edge factor 16"),
+                     desc="PageRank 20 iterations, float ranks (d=0.85), on directed R-MAT scale 20, edge factor 16"),
+    "pagerank_f64": dict(kind="rmat", scale=20, ef=16, weighted=False, symmetric=False,
+                         desc="PageRank 20 iterations, double ranks as the reference, on directed R-MAT scale 20, "
+                              "edge factor 16"),
     "sssp": dict(kind="rmat", scale=25, ef=16, weighted=True, symmetric=False,
                  desc="SSSP (float weights in [0,1)) from seeded roots on R-MAT scale 25, edge factor 16"),
     "bc": dict(kind="rmat", scale=25, ef=16, weighted=False, symmetric=False,
@@ -67,7 +70,7 @@ WORKLOADS = {
                          desc="batched SSSP, 64 seeded roots per launch, on R-MAT scale 24, edge factor 16, "
                               "float weights in [0,1)"),
 }
-REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs",
+REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "pagerank_f64": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs",
            "bfs_batched": "bfs", "sssp_batched": "sssp", "serve": "bfs"}
 
 
@@ -197,8 +200,8 @@ def committed_traffic(kernel, workload):
 def algorithmic_bytes(mode, ae, V, n_frontier, workload):
     """Bytes a call must move (per counted edge: neighbour id + the value it
     gathers or scatters; per vertex: offsets, degree, state; bitmaps)."""
-    per_edge = {"bfs": 8, "bfs_grid": 8, "cc": 8, "sssp": 12, "bc": 12, "pagerank": 12}[workload]
-    state = {"bfs": 4, "bfs_grid": 4, "cc": 4, "sssp": 4, "bc": 8, "pagerank": 8}[workload]
+    per_edge = {"bfs": 8, "bfs_grid": 8, "cc": 8, "sssp": 12, "bc": 12, "pagerank": 8, "pagerank_f64": 12}[workload]
+    state = {"bfs": 4, "bfs_grid": 4, "cc": 4, "sssp": 4, "bc": 8, "pagerank": 4, "pagerank_f64": 8}[workload]
     if mode == 1:   # pull: every vertex's offsets, its state write, three bitmaps
         return per_edge * ae + V * (8 + state) + 3 * (V // 8)
     return per_edge * ae + n_frontier * (8 + 4 + 4)   # push: frontier offsets, degree, queue entry
@@ -218,6 +221,8 @@ def run_once(gg, g, workload, arg, to_host, stats_cls):
     elif workload == "cc":
         _, st = g.cc(to_host=to_host)
     elif workload == "pagerank":
+        _, _, st = g.pagerank(arg, to_host=to_host, f32=True)
+    elif workload == "pagerank_f64":
         _, _, st = g.pagerank(arg, to_host=to_host)
     elif workload == "sssp":
         _, st = g.sssp(arg, to_host=to_host)
@@ -227,7 +232,7 @@ def run_once(gg, g, workload, arg, to_host, stats_cls):
 
 
 def step_args(gg, g, workload, count):
-    if workload == "pagerank":
+    if workload in ("pagerank", "pagerank_f64"):
         return [20] * count
     if workload == "cc":
         return [None] * count
@@ -238,7 +243,7 @@ def step_args(gg, g, workload, count):
 
 # ----------------------------------------------------------------- CPU side
 def ref_sample_scale(workload):
-    return {"bfs": 22, "cc": 21, "pagerank": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024, "bfs_batched": 22,
+    return {"bfs": 22, "cc": 21, "pagerank": 20, "pagerank_f64": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024, "bfs_batched": 22,
             "sssp_batched": 21, "serve": 22}[workload]
 
 
@@ -265,7 +270,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
         args = gg.pick_roots(np.bincount(src, minlength=V), n, seed=SEED + 2000)
     elif workload == "bfs_grid":
         args = [0] * n
-    elif workload == "pagerank":
+    elif workload in ("pagerank", "pagerank_f64"):
         args = [20] * n
     else:
         args = [0] * n
@@ -279,7 +284,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
             tr = og.sssp(a)[1]
         elif workload == "bc":
             tr = og.bc(a)[2]
-        elif workload == "pagerank":
+        elif workload in ("pagerank", "pagerank_f64"):
             tr = og.pagerank(a)[2]
         else:
             tr = og.cc()[1]
@@ -314,7 +319,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
             og.sssp(a)
         elif workload == "bc":
             og.bc(a)
-        elif workload == "pagerank":
+        elif workload in ("pagerank", "pagerank_f64"):
             og.pagerank(a)
         else:
             og.cc()
@@ -337,7 +342,7 @@ def reference_arm(args, dist):
         "impl": "reference", "metric": METRIC, "value": round(r["value"], 4), "unit": "GTEPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * sum(r["times"]) / len(r["times"]), 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f64"}.get(args.workload, "u32"),
+        "scaling": "weak", "vs_baseline": None, "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f32", "pagerank_f64": "f64"}.get(args.workload, "u32"),
         "data": "synthetic", "config": {"workload": w["desc"], "sample": r["sample"]},
         "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": round(r["value"], 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -402,7 +407,7 @@ def gpu_arm(args, dist):
                 "share_of_edge_kernel_time": round(per_mode[dom][0] / total_kernel_ms, 4) if total_kernel_ms else None}
     # ---- e2e through the C ABI with host buffers
     host_out = gg.PinnedArray(V, np.uint32 if args.workload in ("bfs", "bfs_grid", "cc") else
-                              (np.float32 if args.workload == "sssp" else np.float64))
+                              (np.float32 if args.workload in ("sssp", "pagerank") else np.float64))
     dist.barrier()
     e_edges, e_wall = 0, 0.0
     for a in step_in[n:n + args.steps]:
@@ -418,7 +423,7 @@ def gpu_arm(args, dist):
         "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_max * 1000 / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f64"}.get(args.workload, "u32"),
+        "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f32", "pagerank_f64": "f64"}.get(args.workload, "u32"),
         "data": "synthetic (seeded R-MAT / grid generated on the device)",
         "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"],
                    "l2": "inputs larger than L2 (graph %.1f GB)" % (info["device_bytes"] / 1e9),
@@ -649,6 +654,8 @@ def run_once_stats(gg, g, workload, a, st):
     elif workload == "cc":
         gg._check(L.gg_cc(g.h, None, ctypes.byref(st.s)))
     elif workload == "pagerank":
+        gg._check(L.gg_pagerank_f32(g.h, a, None, None, ctypes.byref(st.s)))
+    elif workload == "pagerank_f64":
         gg._check(L.gg_pagerank(g.h, a, None, None, ctypes.byref(st.s)))
     elif workload == "sssp":
         gg._check(L.gg_sssp(g.h, a, None, ctypes.byref(st.s)))
@@ -667,6 +674,8 @@ def run_e2e(gg, g, workload, a, out):
     elif workload == "cc":
         gg._check(L.gg_cc(g.h, p, ctypes.byref(st.s)))
     elif workload == "pagerank":
+        gg._check(L.gg_pagerank_f32(g.h, a, p, None, ctypes.byref(st.s)))
+    elif workload == "pagerank_f64":
         gg._check(L.gg_pagerank(g.h, a, p, None, ctypes.byref(st.s)))
     elif workload == "sssp":
         gg._check(L.gg_sssp(g.h, a, p, ctypes.byref(st.s)))

@@ -88,6 +88,8 @@ def library():
         "gg_server_stats_get": ([vp, ctypes.POINTER(_ServerStats)], i32),
         "gg_server_free": ([vp], i32),
         "gg_pool_bytes": ([vp, i32], u64),
+        "gg_graph_set_bins": ([vp, u32, u32], i32),
+        "gg_autotune": ([vp, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
     for name, (args, res) in sig.items():
@@ -118,6 +120,11 @@ class _ServerStats(ctypes.Structure):
                 ("pools_opened", ctypes.c_uint64), ("pools_closed", ctypes.c_uint64),
                 ("admission_waits", ctypes.c_uint64), ("bytes_in_use", ctypes.c_uint64), ("budget", ctypes.c_uint64),
                 ("max_busy_pools", ctypes.c_int32), ("max_lanes_in_use", ctypes.c_int32)]
+
+
+class _TuneResult(ctypes.Structure):
+    _fields_ = [("light_deg", ctypes.c_uint32), ("pull_chunk", ctypes.c_uint32), ("best_ms", ctypes.c_double),
+                ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32)]
 
 
 class RunStats:
@@ -268,6 +275,14 @@ class Graph:
     @property
     def edges(self):
         return self.info()["edges"]
+
+    def set_bins(self, light_deg, pull_chunk):
+        _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk))
+
+    def autotune(self, cache_dir=None):
+        r = _TuneResult()
+        _check(library().gg_autotune(self.h, os.fsencode(cache_dir) if cache_dir else None, ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in _TuneResult._fields_}
 
     def transpose(self):
         _check(library().gg_graph_transpose(self.h))

@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256)
       const u64 vis = visit[v];
       u64 need = ~vis & alive;
       const unsigned long long b = d.off[v], e = d.off[v + 1];
-      if (need && e - b <= LIGHT_DEG) {
+      if (need && e - b <= d.light) {
         for (unsigned long long k = b; k < e && need; k++) {
           const uint32_t u = d.nbr[k];
           const u64 m = front[u] & need;
@@ -137,9 +137,9 @@ __global__ void __launch_bounds__(256)
     const uint32_t v = d.big[o];
     u64 need = ~visit[v] & alive;
     if (!need) continue;
-    const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * PULL_CHUNK;
+    const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * d.chunk;
     const unsigned long long end = d.off[v + 1];
-    const unsigned long long e = b + PULL_CHUNK < end ? b + PULL_CHUNK : end;
+    const unsigned long long e = b + d.chunk < end ? b + d.chunk : end;
     for (unsigned long long base = b; base < e; base += 32) {
       need &= ~*(volatile u64 *)(next + v);
       if (!need) break;

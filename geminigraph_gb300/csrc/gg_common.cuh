@@ -50,12 +50,14 @@ int cuda_status(cudaError_t e, const char *what);
 // Graph::tune_chunks, core/graph.hpp:1341-1404): pull kernels give a light
 // list (deg <= LIGHT_DEG) one lane, a medium list one warp, and split every
 // heavy list (deg > HEAVY_DEG) into HEAVY_CHUNK-edge chunks, one block each.
-constexpr uint32_t LIGHT_DEG = 32;
+constexpr uint32_t LIGHT_DEG = 32;     // default light-list bound (Dir.light; autotuned)
 constexpr uint32_t HEAVY_DEG = 2048;
 constexpr uint32_t HEAVY_CHUNK = 2048;
-constexpr uint32_t PULL_CHUNK = 256;   // reduction pulls: edges per warp work item
+constexpr uint32_t PULL_CHUNK = 256;   // default reduction-pull chunk (Dir.chunk; autotuned)
 
 struct Dir {
+  uint32_t light = LIGHT_DEG;       // lists up to this long are "light" (one lane)
+  uint32_t chunk = PULL_CHUNK;      // edges per warp work item of the reduction pulls
   uint64_t *off = nullptr;
   uint32_t *nbr = nullptr;
   float *w = nullptr;

@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
     }
     uint32_t deg = (uint32_t)(e - b);
     bool a = false;
-    if (todo && deg <= LIGHT_DEG) {
+    if (todo && deg <= d.light) {
       // four independent gathers in flight, combined in list order
       Acc acc = op.identity(v);
       unsigned long long k = b;
@@ -214,13 +214,13 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
   t.flush(ctr);
 }
 
-// Lists longer than LIGHT_DEG: one warp per PULL_CHUNK-edge chunk, eight
-// independent gathers in flight per lane; partials[c] = the chunk's combine.
-template <class Op>
+// Lists longer than d.light: one warp per d.chunk-edge chunk (d.chunk =
+// 32 * PER_LANE, 128 / 256 / 512), PER_LANE independent gathers per lane;
+// partials[c] = the chunk's combine.
+template <class Op, int PER_LANE>
 __global__ void __launch_bounds__(PULL_THREADS)
     pull_chunks(Dir d, Op op, typename Op::Acc *__restrict__ partials) {
   using Acc = typename Op::Acc;
-  constexpr int PER_LANE = PULL_CHUNK / 32;
   const size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
   const unsigned lane = lane_id();
   for (size_t c = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); c < d.nbigchunks; c += nwarps) {
@@ -228,9 +228,9 @@ __global__ void __launch_bounds__(PULL_THREADS)
     const uint32_t v = d.big[o];
     Acc part = op.identity_coop();
     if (op.want(v)) {
-      const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * PULL_CHUNK;
+      const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * (32 * PER_LANE);
       const unsigned long long end = d.off[v + 1];
-      const unsigned long long e = b + PULL_CHUNK < end ? b + PULL_CHUNK : end;
+      const unsigned long long e = b + 32 * PER_LANE < end ? b + 32 * PER_LANE : end;
       Acc vals[PER_LANE];
 #pragma unroll
       for (int j = 0; j < PER_LANE; j++) {
@@ -332,7 +332,7 @@ static __global__ void __launch_bounds__(PULL_THREADS, 8)
     const uint32_t v = (uint32_t)(g * 32 + lane);
     uint32_t found = NONE32;
     if (todo) {
-      unsigned long long lim = e - b <= LIGHT_DEG ? e : b + LIGHT_DEG;
+      unsigned long long lim = e - b <= d.light ? e : b + d.light;
       for (unsigned long long k = b; k < lim && found == NONE32; k += 4) {
         uint32_t s0 = d.nbr[k];
         uint32_t s1 = k + 1 < lim ? d.nbr[k + 1] : s0;
@@ -374,7 +374,7 @@ static __global__ void __launch_bounds__(PULL_THREADS)
     uint32_t v = d.med[i];
     uint32_t found = NONE32;
     if (!bm_test(act.visited, v)) {
-      unsigned long long b = d.off[v] + LIGHT_DEG, e = d.off[v + 1];
+      unsigned long long b = d.off[v] + d.light, e = d.off[v + 1];
       for (unsigned long long base = b; base < e; base += 32) {
         unsigned long long k = base + lane;
         uint32_t s = 0;
@@ -693,8 +693,13 @@ struct Launch {
     if (d.nbig) {
       typename Op::Acc *part = nullptr;
       GG_TRY(ws(g, WS_PARTIAL, d.nbigchunks, &part));
-      pull_chunks<Op><<<grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(
-          d, op, part);
+      const unsigned cg = grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, 8);
+      if (d.chunk == 128)
+        pull_chunks<Op, 4><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+      else if (d.chunk == 512)
+        pull_chunks<Op, 16><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+      else
+        pull_chunks<Op, 8><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
       pull_big_finish<Op><<<grid_for(d.nbig, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, op, part, act,
                                                                                                   ctr);
       launches += 2;

@@ -427,11 +427,46 @@ static int chunk_table(gg_graph *g, const Dir *d, const uint32_t *list, uint32_t
 
 // Degree bins of one direction (see Dir).
 static int build_bins(gg_graph *g, Dir *d) {
-  GG_TRY(bin_list(g, d, LIGHT_DEG, HEAVY_DEG, &d->med, &d->nmed));
+  GG_TRY(bin_list(g, d, d->light, HEAVY_DEG, &d->med, &d->nmed));
   GG_TRY(bin_list(g, d, HEAVY_DEG, 0xffffffffu, &d->heavy, &d->nheavy));
   GG_TRY(chunk_table(g, d, d->heavy, d->nheavy, HEAVY_CHUNK, &d->heavy_chunk, &d->chunk_owner, &d->nchunks));
-  GG_TRY(bin_list(g, d, LIGHT_DEG, 0xffffffffu, &d->big, &d->nbig));
-  GG_TRY(chunk_table(g, d, d->big, d->nbig, PULL_CHUNK, &d->big_chunk, &d->big_owner, &d->nbigchunks));
+  GG_TRY(bin_list(g, d, d->light, 0xffffffffu, &d->big, &d->nbig));
+  GG_TRY(chunk_table(g, d, d->big, d->nbig, d->chunk, &d->big_chunk, &d->big_owner, &d->nbigchunks));
+  return GG_OK;
+}
+
+static void free_bins(gg_graph *g, Dir *d) {
+  g->graph_bytes -= sizeof(uint32_t) * ((size_t)d->nmed + d->nheavy + d->nheavy + 1 + d->nchunks + d->nbig +
+                                        d->nbig + 1 + d->nbigchunks);
+  uint32_t *lists[] = {d->med, d->heavy, d->heavy_chunk, d->chunk_owner, d->big, d->big_chunk, d->big_owner};
+  for (uint32_t *p : lists)
+    if (p) cudaFree(p);
+  d->med = d->heavy = d->heavy_chunk = d->chunk_owner = d->big = d->big_chunk = d->big_owner = nullptr;
+  d->nmed = d->nheavy = d->nchunks = d->nbig = d->nbigchunks = 0;
+}
+
+// Rebuilds both directions' degree bins for a light-list bound and a pull
+// chunk size (the autotuner's two knobs).
+int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk) {
+  if (light < 1 || light > HEAVY_DEG || (chunk != 128 && chunk != 256 && chunk != 512)) {
+    set_error("light list bound must be 1..%u and the pull chunk 128, 256 or 512", HEAVY_DEG);
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  const bool alias = g->in.nbr == g->out.nbr;
+  free_bins(g, &g->out);
+  g->out.light = light;
+  g->out.chunk = chunk;
+  GG_TRY(build_bins(g, &g->out));
+  if (alias) {
+    g->in = g->out;
+  } else {
+    free_bins(g, &g->in);
+    g->in.light = light;
+    g->in.chunk = chunk;
+    GG_TRY(build_bins(g, &g->in));
+  }
   return GG_OK;
 }
 

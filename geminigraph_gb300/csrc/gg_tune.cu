@@ -1,0 +1,169 @@
+// Autotuner for the degree bins: the light-list bound (lists up to it get one
+// lane) and the reduction-pull chunk (edges per warp work item).  The best
+// pair depends on the graph's degree distribution, so it is measured on the
+// graph itself: every candidate rebuilds the bins and times two float
+// PageRank iterations (light and chunked pulls) plus one BFS from the vertex
+// of largest out-degree (push, pull, small runs) with CUDA events; the
+// fastest is kept and recorded in a cache file keyed by a fingerprint of the
+// graph, so the next load of the same graph skips the search.
+#include <stdio.h>
+#include <stdlib.h>
+#include <sys/stat.h>
+
+#include <string>
+#include <vector>
+
+#include "gg_common.cuh"
+#include "gg_gen.h"
+
+namespace gg {
+
+int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk);
+
+__global__ void degree_fingerprint(const uint32_t *__restrict__ out_deg, const uint32_t *__restrict__ in_deg,
+                                   uint32_t V, unsigned long long *out, unsigned *argmax_deg) {
+  unsigned long long h = 0;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t o = out_deg[v], i = in_deg[v];
+    h += gg_mix64((unsigned long long)v * 0x9E3779B97F4A7C15ull + ((unsigned long long)o << 32 | i));
+    atomicMax(argmax_deg, o);
+  }
+  h = warp_sum(h);
+  if (lane_id() == 0) atomicAdd(out, h);
+}
+
+__global__ void find_vertex_with_degree(const uint32_t *__restrict__ out_deg, uint32_t V, unsigned target,
+                                        unsigned *vertex) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    if (out_deg[v] == target) atomicMin(vertex, (unsigned)v);
+}
+
+static std::string cache_file(const char *dir) {
+  std::string d;
+  if (dir && *dir) {
+    d = dir;
+  } else if (getenv("GG_TUNE_CACHE")) {
+    d = getenv("GG_TUNE_CACHE");
+  } else if (getenv("HOME")) {
+    d = std::string(getenv("HOME")) + "/.cache/geminigraph_gb300";
+  } else {
+    d = "/tmp/geminigraph_gb300";
+  }
+  return d + "/bins_v1.txt";
+}
+
+static void mkdirs(const std::string &path) {
+  for (size_t i = 1; i < path.size(); i++)
+    if (path[i] == '/') mkdir(path.substr(0, i).c_str(), 0755);
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  return rebuild_bins(g, light_deg, pull_chunk);
+}
+
+int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  GG_CUDA(cudaSetDevice(g->device));
+  // fingerprint and the BFS root of the timing run
+  unsigned long long *d_h;
+  unsigned *d_m;
+  GG_CUDA(cudaMalloc(&d_h, sizeof(unsigned long long) + 2 * sizeof(unsigned)));
+  d_m = (unsigned *)(d_h + 1);
+  GG_CUDA(cudaMemsetAsync(d_h, 0, sizeof(unsigned long long) + sizeof(unsigned), g->stream));
+  GG_CUDA(cudaMemsetAsync(d_m + 1, 0xff, sizeof(unsigned), g->stream));
+  degree_fingerprint<<<grid_for(g->V, 256, g->num_sms, 8), 256, 0, g->stream>>>(g->out.deg, g->in.deg, g->V, d_h,
+                                                                              d_m);
+  unsigned long long h = 0;
+  unsigned hm[2] = {0, 0};
+  GG_CUDA(cudaMemcpyAsync(hm, d_m, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  find_vertex_with_degree<<<grid_for(g->V, 256, g->num_sms, 8), 256, 0, g->stream>>>(g->out.deg, g->V, hm[0],
+                                                                                   d_m + 1);
+  GG_CUDA(cudaMemcpyAsync(&h, d_h, sizeof(h), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaMemcpyAsync(hm + 1, d_m + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  cudaFree(d_h);
+  const uint32_t root = hm[1] < g->V ? hm[1] : 0;
+  char key[160];
+  snprintf(key, sizeof(key), "%u:%llu:%llu:%d:%d:%016llx", g->V, (unsigned long long)g->E,
+           (unsigned long long)g->nadj, g->weighted, g->symmetric, h);
+  gg_tune_result r;
+  memset(&r, 0, sizeof(r));
+  // cached?
+  const std::string file = cache_file(cache_dir);
+  if (FILE *f = fopen(file.c_str(), "r")) {
+    char k[160];
+    unsigned light, chunk;
+    double ms;
+    while (fscanf(f, "%159s %u %u %lf", k, &light, &chunk, &ms) == 4) {
+      if (std::string(k) == key) {
+        r.light_deg = light;
+        r.pull_chunk = chunk;
+        r.best_ms = ms;
+        r.from_cache = 1;
+      }
+    }
+    fclose(f);
+    if (r.from_cache) {
+      GG_TRY(rebuild_bins(g, r.light_deg, r.pull_chunk));
+      if (out) *out = r;
+      return GG_OK;
+    }
+  }
+  const uint32_t lights[] = {16, 32, 64};
+  const uint32_t chunks[] = {128, 256, 512};
+  auto measure = [&](double *ms) -> int {
+    gg_run_stats st;
+    memset(&st, 0, sizeof(st));
+    double t = 0;
+    GG_TRY(gg_pagerank_f32(g, 2, nullptr, nullptr, &st));
+    t += st.device_ms;
+    GG_TRY(gg_bfs(g, root, nullptr, &st));
+    t += st.device_ms;
+    *ms = t;
+    return GG_OK;
+  };
+  double best = 1e300, def = 0;
+  uint32_t bl = LIGHT_DEG, bc = PULL_CHUNK;
+  for (uint32_t light : lights)
+    for (uint32_t chunk : chunks) {
+      GG_TRY(rebuild_bins(g, light, chunk));
+      double ms0, ms1;
+      GG_TRY(measure(&ms0));  // warm
+      GG_TRY(measure(&ms1));
+      r.candidates += 1;
+      if (light == LIGHT_DEG && chunk == PULL_CHUNK) def = ms1;
+      if (ms1 < best) {
+        best = ms1;
+        bl = light;
+        bc = chunk;
+      }
+    }
+  GG_TRY(rebuild_bins(g, bl, bc));
+  r.light_deg = bl;
+  r.pull_chunk = bc;
+  r.best_ms = best;
+  r.default_ms = def;
+  mkdirs(file);
+  if (FILE *f = fopen(file.c_str(), "a")) {
+    fprintf(f, "%s %u %u %.6f\n", key, bl, bc, best);
+    fclose(f);
+  }
+  if (out) *out = r;
+  return GG_OK;
+}
+
+}  // extern "C"

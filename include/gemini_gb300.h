@@ -213,6 +213,29 @@ int gg_server_free(gg_server *s);
  * 1 secondary (inv_num_paths).  Valid until the next toolkit call on g. */
 const void *gg_result_device_ptr(const gg_graph *g, int which);
 
+/* ---- autotuner (no counterpart in the reference; Graph::tune_chunks,
+ * core/graph.hpp:1341-1404, balances threads by edge counts at load) ----
+ * The pull kernels split vertices into light lists (<= light_deg entries, one
+ * lane each) and longer lists cut into pull_chunk-edge warp work items.
+ * gg_graph_set_bins sets both (light_deg 1..2048; pull_chunk 128, 256 or 512);
+ * gg_autotune times 9 candidate pairs on the graph itself (two float PageRank
+ * iterations and one BFS per candidate, CUDA events), keeps the fastest and
+ * records it in <cache_dir>/bins_v1.txt (cache_dir NULL: $GG_TUNE_CACHE, else
+ * ~/.cache/geminigraph_gb300) under a fingerprint of the graph; a later call on
+ * the same graph reads the cache instead of searching.  Results of every
+ * toolkit are independent of the bins. */
+typedef struct {
+  uint32_t light_deg;
+  uint32_t pull_chunk;
+  double best_ms;        /* timing workload with the chosen pair */
+  double default_ms;     /* the same with the defaults (32, 256) */
+  int32_t candidates;    /* pairs timed (0 when read from the cache) */
+  int32_t from_cache;
+} gg_tune_result;
+
+int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk);
+int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out);
+
 /* ---- engine primitives ---- */
 
 /* Graph::process_vertices (core/graph.hpp:1406-1469) for the reduction

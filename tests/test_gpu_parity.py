@@ -331,3 +331,43 @@ def test_pull_bins_cover_all_degrees():
     lab, _ = gs.cc()
     olab, _ = OracleGraph(V, s, d, symmetric=True).cc()
     assert np.array_equal(lab, olab)
+
+
+@pytest.mark.parametrize("light,chunk", [(16, 128), (64, 512), (1, 256)])
+def test_results_do_not_depend_on_bins(light, chunk):
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d, w)
+    g.set_bins(light, chunk)
+    o = OracleGraph(V, s, d, w)
+    parent, st = g.bfs(root)
+    op, otr = o.bfs(root)
+    assert st.rows() == otr and np.array_equal(bfs_levels(parent, root), bfs_levels(op, root))
+    ranks, _, _ = g.pagerank(10)
+    assert rel_l1(ranks, o.pagerank(10)[0]) < PR_TOL
+    dist, _ = g.sssp(root)
+    assert np.array_equal(dist.view(np.uint32), o.sssp(root)[0].view(np.uint32))
+    dep, inv, _ = g.bc(root)
+    odep, oinv, _ = o.bc(root)
+    ok = ~np.isnan(odep)
+    assert rel_l1(dep[ok], odep[ok]) < BC_TOL
+    lv, _, _, _, _ = gg.bfs_batched(g, [root, 0, 5])
+    assert np.array_equal(lv[0], bfs_levels(op, root))
+    gs = gg.Graph.from_edges(V, s, d, symmetric=True)
+    gs.set_bins(light, chunk)
+    assert np.array_equal(gs.cc()[0], OracleGraph(V, s, d, symmetric=True).cc()[0])
+
+
+def test_autotune_picks_and_caches(tmp_path):
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d, w)
+    r1 = g.autotune(str(tmp_path))
+    assert r1["candidates"] == 9 and r1["from_cache"] == 0
+    assert r1["light_deg"] in (16, 32, 64) and r1["pull_chunk"] in (128, 256, 512)
+    assert r1["best_ms"] <= r1["default_ms"]
+    g2 = gg.Graph.from_edges(V, s, d, w)
+    r2 = g2.autotune(str(tmp_path))
+    assert r2["from_cache"] == 1 and (r2["light_deg"], r2["pull_chunk"]) == (r1["light_deg"], r1["pull_chunk"])
+    parent, st = g2.bfs(root)
+    assert st.rows() == OracleGraph(V, s, d).bfs(root)[1]
+    with pytest.raises(gg.GeminiError):
+        g2.set_bins(32, 300)

@@ -89,6 +89,7 @@ def library():
         "gg_server_free": ([vp], i32),
         "gg_pool_bytes": ([vp, i32], u64),
         "gg_graph_set_bins": ([vp, u32, u32], i32),
+        "gg_graph_set_pr_layout": ([vp, i32], i32),
         "gg_autotune": ([vp, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
@@ -278,6 +279,9 @@ class Graph:
 
     def set_bins(self, light_deg, pull_chunk):
         _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk))
+
+    def set_pr_layout(self, hot_sources):
+        _check(library().gg_graph_set_pr_layout(self.h, 1 if hot_sources else 0))
 
     def autotune(self, cache_dir=None):
         r = _TuneResult()

@@ -133,13 +133,11 @@ __global__ void __launch_bounds__(256)
   const size_t nwarps = (size_t)gridDim.x * 8;
   const unsigned lane = lane_id();
   for (size_t c = (size_t)blockIdx.x * 8 + (threadIdx.x >> 5); c < d.nbigchunks; c += nwarps) {
-    const uint32_t o = d.big_owner[c];
-    const uint32_t v = d.big[o];
+    uint32_t v;
+    unsigned long long lo, b, e;
+    big_range(d, (uint32_t)c, d.chunk, &v, &lo, &b, &e);
     u64 need = ~visit[v] & alive;
     if (!need) continue;
-    const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * d.chunk;
-    const unsigned long long end = d.off[v + 1];
-    const unsigned long long e = b + d.chunk < end ? b + d.chunk : end;
     for (unsigned long long base = b; base < e; base += 32) {
       need &= ~*(volatile u64 *)(next + v);
       if (!need) break;

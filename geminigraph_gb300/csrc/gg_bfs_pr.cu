@@ -133,7 +133,7 @@ struct PrPull {
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
   __device__ __forceinline__ T identity(uint32_t) const { return T(0); }
   __device__ __forceinline__ T identity_coop() const { return T(0); }
-  __device__ __forceinline__ T gather(const Dir &d, unsigned long long k) const { return curr[d.nbr[k]]; }
+  __device__ __forceinline__ T gather(const Dir &, unsigned long long, uint32_t u) const { return curr[u]; }
   __device__ __forceinline__ T combine(T a, T b) const { return a + b; }
   __device__ __forceinline__ T warp_combine(T x) const { return warp_sum(x); }
   __device__ __forceinline__ bool finish(uint32_t v, T sum, uint32_t, Tally &t) const;
@@ -181,6 +181,18 @@ __global__ void pr_init(T *curr, const uint32_t *out_deg, uint32_t V) {
   }
 }
 
+// Ranks computed in the hot-source numbering back to vertex order.
+template <typename T>
+__global__ void pr_unrank(const T *__restrict__ by_rank, const uint32_t *__restrict__ rank_of, uint32_t V,
+                          T *__restrict__ out) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    out[v] = by_rank[rank_of[v]];
+}
+
+// pagerank.cpp:35-97.  With the hot-source layout (the default) the
+// iterations run in that numbering: pr_od is the out-degree there, every
+// vertex's arithmetic is unchanged, and only the order in which an in-list
+// is summed differs from the plain adjacency (by source number).
 template <typename T>
 static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_host, gg_run_stats *st) {
   if (iterations < 0) {
@@ -188,9 +200,14 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
     return GG_ERR_INVALID;
   }
   GG_CUDA(cudaSetDevice(g->device));
+  if (g->pr_layout) GG_TRY(pr_layout_build(g));
+  const bool ranked = g->pr_layout && g->pr_ready;
+  const Dir &din = ranked ? g->pr : g->in;
+  const uint32_t *od = ranked ? g->pr_od : g->out.deg;
   const uint32_t V = g->V;
-  T *buf[2];
+  T *buf[2], *out = nullptr;
   Counters *per_iter;
+  if (ranked) GG_TRY(ws(g, WS_S0, (size_t)V, &out));
   GG_TRY(ws(g, WS_S2, (size_t)V, &buf[0]));
   GG_TRY(ws(g, WS_S3, (size_t)V, &buf[1]));
   GG_TRY(ws(g, WS_HUBSUM, (size_t)(iterations > 0 ? iterations : 1), &per_iter));
@@ -199,19 +216,25 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
   cudaStream_t s = g->stream;
   GG_TRY(timed_begin(g));
   GG_CUDA(cudaMemsetAsync(per_iter, 0, sizeof(Counters) * (iterations > 0 ? iterations : 1), s));
-  pr_init<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[0], g->out.deg, V);
+  pr_init<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[0], od, V);
   L.launches += 1;
   int cur = 0;
   // active = all: active_edges = sum of out_degree = adjacency entries
   unsigned long long ae = g->nadj;
   for (int i = 0; i < iterations; i++) {
     tr.add(ae < g->E / 20 ? 0 : 1, ae, V);
-    PrPull<T> op{buf[cur], buf[cur ^ 1], g->out.deg, i == iterations - 1};
+    PrPull<T> op{buf[cur], buf[cur ^ 1], od, i == iterations - 1};
     GG_TRY(tr.kbegin());
-    GG_TRY(L.pull(g->in, op, ActOut(), per_iter + i));
+    GG_TRY(L.pull(din, op, ActOut(), per_iter + i));
     GG_TRY(tr.kend());
     GG_CUDA(cudaGetLastError());
     cur ^= 1;
+  }
+  const T *result = buf[cur];
+  if (ranked) {
+    pr_unrank<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[cur], g->pr_rank_of, V, out);
+    L.launches += 1;
+    result = out;
   }
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
@@ -225,8 +248,8 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
     delete[] hc;
     GG_CUDA(e);
   }
-  if (ranks_host) GG_CUDA(cudaMemcpy(ranks_host, buf[cur], sizeof(T) * V, cudaMemcpyDeviceToHost));
-  g->result[0] = buf[cur];
+  if (ranks_host) GG_CUDA(cudaMemcpy(ranks_host, result, sizeof(T) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = result;
   g->result[1] = nullptr;
   return GG_OK;
 }
@@ -259,6 +282,16 @@ int gg_bfs(gg_graph *g, uint32_t root, uint32_t *parent, gg_run_stats *stats) {
     return GG_ERR_INVALID;
   }
   return bfs_run(g, root, parent, stats);
+}
+
+int gg_graph_set_pr_layout(gg_graph *g, int hot_sources) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  g->pr_layout = hot_sources ? 1 : 0;
+  if (!g->pr_layout) pr_layout_free(g);
+  return GG_OK;
 }
 
 int gg_pagerank(gg_graph *g, int iterations, double *ranks, double *deltas, gg_run_stats *stats) {

@@ -31,7 +31,7 @@ struct CcPull {
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
   __device__ __forceinline__ uint32_t identity(uint32_t v) const { return v; }
   __device__ __forceinline__ uint32_t identity_coop() const { return 0xffffffffu; }
-  __device__ __forceinline__ uint32_t gather(const Dir &d, unsigned long long k) const { return cur[d.nbr[k]]; }
+  __device__ __forceinline__ uint32_t gather(const Dir &, unsigned long long, uint32_t u) const { return cur[u]; }
   __device__ __forceinline__ uint32_t combine(uint32_t a, uint32_t b) const { return b < a ? b : a; }
   __device__ __forceinline__ uint32_t warp_combine(uint32_t x) const { return warp_min(x); }
   __device__ __forceinline__ bool finish(uint32_t v, uint32_t m, uint32_t, Tally &) const {
@@ -78,8 +78,8 @@ struct SsspPull {
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
   __device__ __forceinline__ float identity(uint32_t) const { return 1e9f; }
   __device__ __forceinline__ float identity_coop() const { return 1e9f; }
-  __device__ __forceinline__ float gather(const Dir &d, unsigned long long k) const {
-    return __fadd_rn(cur[d.nbr[k]], d.w[k]);
+  __device__ __forceinline__ float gather(const Dir &d, unsigned long long k, uint32_t u) const {
+    return __fadd_rn(cur[u], d.w[k]);
   }
   __device__ __forceinline__ float combine(float a, float b) const { return b < a ? b : a; }
   __device__ __forceinline__ float warp_combine(float x) const { return warp_min(x); }
@@ -272,8 +272,7 @@ struct BcFwdPull {
   __device__ __forceinline__ bool want(uint32_t v) const { return !bm_test(visited, v); }
   __device__ __forceinline__ double identity(uint32_t) const { return 0.0; }
   __device__ __forceinline__ double identity_coop() const { return 0.0; }
-  __device__ __forceinline__ double gather(const Dir &d, unsigned long long k) const {
-    uint32_t s = d.nbr[k];
+  __device__ __forceinline__ double gather(const Dir &, unsigned long long, uint32_t s) const {
     return bm_test_ldg(active_in, s) ? np[s] : 0.0;
   }
   __device__ __forceinline__ double combine(double a, double b) const { return a + b; }
@@ -307,8 +306,7 @@ struct BcBwdPull {
   __device__ __forceinline__ bool want(uint32_t v) const { return !bm_test(visited, v); }
   __device__ __forceinline__ double identity(uint32_t) const { return 0.0; }
   __device__ __forceinline__ double identity_coop() const { return 0.0; }
-  __device__ __forceinline__ double gather(const Dir &d, unsigned long long k) const {
-    uint32_t s = d.nbr[k];
+  __device__ __forceinline__ double gather(const Dir &, unsigned long long, uint32_t s) const {
     return bm_test_ldg(level, s) ? dep[s] : 0.0;
   }
   __device__ __forceinline__ double combine(double a, double b) const { return a + b; }

@@ -72,7 +72,7 @@ struct Dir {
   uint32_t nchunks = 0;
   uint32_t *big = nullptr;          // deg > LIGHT_DEG, ascending (reduction pulls)
   uint32_t nbig = 0;
-  uint32_t *big_chunk = nullptr;    // nbig+1: prefix of per-vertex PULL_CHUNK counts
+  uint32_t *big_chunk = nullptr;    // nbig+1: prefix of per-vertex chunk counts (aligned blocks, see big_range)
   uint32_t *big_owner = nullptr;    // nbigchunks: index into big of each chunk
   uint32_t nbigchunks = 0;
 };
@@ -117,6 +117,8 @@ struct Workspace {
 
 class LanePool;
 void pools_destroy(gg_graph *g);
+int pr_layout_build(gg_graph *g);
+void pr_layout_free(gg_graph *g);
 
 }  // namespace gg
 
@@ -136,6 +138,15 @@ struct gg_graph {
   std::vector<cudaEvent_t> evpool;  // events for per-call kernel timing
   gg::LanePool *pool_bfs = nullptr;  // lane pools of the batched calls
   gg::LanePool *pool_sssp = nullptr;
+  // PageRank's hot-source layout of the incoming adjacency (built on the
+  // first PageRank call, dropped by transpose): vertices renumbered by
+  // descending out-degree, so the ranks gathered most often sit together.
+  gg::Dir pr;
+  uint32_t *pr_rank_of = nullptr;     // V: new number of vertex v
+  uint32_t *pr_id_of_rank = nullptr;  // V: vertex with new number r
+  uint32_t *pr_od = nullptr;          // V: out-degree in the new numbering
+  bool pr_ready = false;
+  int pr_layout = 1;                  // 0: PageRank pulls the plain incoming adjacency
 };
 
 namespace gg {
@@ -220,6 +231,50 @@ __device__ __forceinline__ bool bm_set_atomic(uint32_t *bm, uint32_t v) {
 }
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Chunk c of the long-list table: owner vertex v, aligned block start lo
+// (a multiple of chunk in the adjacency array) and the list's part [b, e)
+// inside [lo, lo + chunk).
+__device__ __forceinline__ void big_range(const Dir &d, uint32_t c, uint32_t chunk, uint32_t *v,
+                                          unsigned long long *lo, unsigned long long *b,
+                                          unsigned long long *e) {
+  const uint32_t o = d.big_owner[c];
+  *v = d.big[o];
+  const unsigned long long b0 = d.off[*v], e0 = d.off[*v + 1];
+  *lo = (b0 / chunk + (c - d.big_chunk[o])) * (unsigned long long)chunk;
+  *b = b0 > *lo ? b0 : *lo;
+  *e = e0 < *lo + chunk ? e0 : *lo + chunk;
+}
+
+// L2 eviction hints.  Adjacency streams through once per sweep and is loaded
+// evict-first (and not kept in L1); vertex state gathered at random is loaded
+// evict-last so that the hot (high out-degree) sources stay in L2 while the
+// adjacency streams past them.
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint32_t ld_stream_u32(const uint32_t *p, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_keep_f32(const float *p, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_keep_f64(const double *p, uint64_t pol) {
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 
 template <typename T>

@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 // ---------------------------------------------------------------- pull
 // Dense mode (core/graph.hpp:1664-1855), reduction form.  For each vertex v
 // with op.want(v): acc = op.identity(v) combined (op.combine) with
-// op.gather(d, k) over its in-list, then op.finish(v, acc, deg, tally)
+// op.gather(d, k, u) (u = the k-th entry) over its in-list, then op.finish(v, acc, deg, tally)
 // applies the slot and returns whether v is activated.  Op::Acc is the
 // message type; op.identity_coop() is the neutral element of combine.
 // Work is split by the direction's degree bins:
@@ -203,10 +203,12 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
       Acc acc = op.identity(v);
       unsigned long long k = b;
       for (; k + 4 <= e; k += 4) {
-        Acc g0 = op.gather(d, k), g1 = op.gather(d, k + 1), g2 = op.gather(d, k + 2), g3 = op.gather(d, k + 3);
+        const uint32_t u0 = d.nbr[k], u1 = d.nbr[k + 1], u2 = d.nbr[k + 2], u3 = d.nbr[k + 3];
+        Acc g0 = op.gather(d, k, u0), g1 = op.gather(d, k + 1, u1), g2 = op.gather(d, k + 2, u2),
+            g3 = op.gather(d, k + 3, u3);
         acc = op.combine(op.combine(op.combine(op.combine(acc, g0), g1), g2), g3);
       }
-      for (; k < e; k++) acc = op.combine(acc, op.gather(d, k));
+      for (; k < e; k++) acc = op.combine(acc, op.gather(d, k, d.nbr[k]));
       a = op.finish(v, acc, deg, t);
     }
     if (act.active_out) pull_activate(a, v, g, act, t);
@@ -214,28 +216,38 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
   t.flush(ctr);
 }
 
-// Lists longer than d.light: one warp per d.chunk-edge chunk (d.chunk =
-// 32 * PER_LANE, 128 / 256 / 512), PER_LANE independent gathers per lane;
-// partials[c] = the chunk's combine.
+// Lists longer than d.light: one warp per d.chunk-edge aligned block of the
+// adjacency (d.chunk = 32 * PER_LANE, 128 / 256 / 512).  Lane l loads the
+// block's 16-byte windows l, l + 32, ... with one vector load each and
+// gathers the entries that belong to the list; partials[c] = the chunk's
+// combine (lane order, then the warp tree).
 template <class Op, int PER_LANE>
 __global__ void __launch_bounds__(PULL_THREADS)
     pull_chunks(Dir d, Op op, typename Op::Acc *__restrict__ partials) {
   using Acc = typename Op::Acc;
+  constexpr int WIN = PER_LANE / 4;
   const size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
   const unsigned lane = lane_id();
   for (size_t c = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); c < d.nbigchunks; c += nwarps) {
-    const uint32_t o = d.big_owner[c];
-    const uint32_t v = d.big[o];
+    uint32_t v;
+    unsigned long long lo, b, e;
+    big_range(d, (uint32_t)c, 32 * PER_LANE, &v, &lo, &b, &e);
     Acc part = op.identity_coop();
     if (op.want(v)) {
-      const unsigned long long b = d.off[v] + (unsigned long long)(c - d.big_chunk[o]) * (32 * PER_LANE);
-      const unsigned long long end = d.off[v + 1];
-      const unsigned long long e = b + 32 * PER_LANE < end ? b + 32 * PER_LANE : end;
+      uint4 w[WIN];
+#pragma unroll
+      for (int i = 0; i < WIN; i++) {
+        const unsigned long long p = lo + 4 * (lane + 32 * i);
+        w[i] = p < e && p + 4 > b ? __ldg(reinterpret_cast<const uint4 *>(d.nbr + p)) : make_uint4(0, 0, 0, 0);
+      }
       Acc vals[PER_LANE];
 #pragma unroll
-      for (int j = 0; j < PER_LANE; j++) {
-        unsigned long long k = b + lane + 32 * j;
-        vals[j] = k < e ? op.gather(d, k) : op.identity_coop();
+      for (int i = 0; i < WIN; i++) {
+        const unsigned long long p = lo + 4 * (lane + 32 * i);
+        const uint32_t u[4] = {w[i].x, w[i].y, w[i].z, w[i].w};
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          vals[4 * i + j] = p + j >= b && p + j < e ? op.gather(d, p + j, u[j]) : op.identity_coop();
       }
 #pragma unroll
       for (int j = 0; j < PER_LANE; j++) part = op.combine(part, vals[j]);

@@ -234,6 +234,17 @@ typedef struct {
 } gg_tune_result;
 
 int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk);
+
+/* PageRank's adjacency layout (no reference counterpart; the reference pulls
+ * its CSC as loaded).  hot_sources = 1 (the default): on its first call
+ * gg_pagerank / gg_pagerank_f32 build, and keep with the graph, a copy of the
+ * incoming adjacency with vertices renumbered by descending out-degree and
+ * each in-list sorted by the new numbers; the iterations run there and the
+ * ranks are mapped back to vertex order.  Sums then run in that order, so
+ * ranks differ from the plain layout's in the last bits only.  hot_sources =
+ * 0 frees the copy and pulls the plain incoming adjacency.  The copy is
+ * dropped by gg_graph_transpose and counted in device_bytes. */
+int gg_graph_set_pr_layout(gg_graph *g, int hot_sources);
 int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out);
 
 /* ---- engine primitives ---- */

@@ -371,3 +371,30 @@ def test_autotune_picks_and_caches(tmp_path):
     assert st.rows() == OracleGraph(V, s, d).bfs(root)[1]
     with pytest.raises(gg.GeminiError):
         g2.set_bins(32, 300)
+
+
+@pytest.mark.parametrize("name", ["rmat16", "grid128", "random_odd"])
+def test_pagerank_layouts_agree(name):
+    """The hot-source layout (default) and the plain incoming adjacency give
+    the same ranks up to summation order, both within tolerance of the
+    oracle; the layout is rebuilt after a transpose and freed on request."""
+    V, s, d, w, _ = case(name)
+    g = gg.Graph.from_edges(V, s, d)
+    oranks = OracleGraph(V, s, d).pagerank(20)[0]
+    hot, _, st = g.pagerank(20)
+    bytes_hot = g.info()["device_bytes"]
+    g.set_pr_layout(False)
+    plain, _, st2 = g.pagerank(20)
+    assert g.info()["device_bytes"] < bytes_hot
+    assert st.rows() == st2.rows()
+    assert rel_l1(hot, oranks) < PR_TOL and rel_l1(plain, oranks) < PR_TOL
+    assert rel_l1(hot, plain) < 1e-13
+    f_plain, _, _ = g.pagerank(20, f32=True)
+    g.set_pr_layout(True)
+    f_hot, _, _ = g.pagerank(20, f32=True)
+    assert rel_l1(f_hot.astype(np.float64), oranks) < PR_F32_TOL
+    assert rel_l1(f_hot.astype(np.float64), f_plain.astype(np.float64)) < 1e-5
+    g.transpose()
+    g.transpose()
+    again, _, _ = g.pagerank(20)
+    assert np.array_equal(again, hot)

@@ -351,6 +351,22 @@ def reference_arm(args, dist):
     return 0
 
 
+def tune_bins(g, args):
+    """Degree bins for this graph: the library defaults, or the autotuner's
+    pick for the workload's kernels (timed on the graph, cached on disk)."""
+    if args.bins == "default":
+        return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1}
+    objective = ("pagerank",) if args.workload.startswith("pagerank") else \
+        ("batched",) if args.workload in ("bfs_batched", "sssp_batched", "serve") else \
+        ("bfs",) if args.workload.startswith("bfs") else ("pagerank", "bfs")
+    t0 = time.perf_counter()
+    r = g.autotune(objective=objective)
+    return {"source": "autotune(%s)" % "+".join(objective), "light_deg": r["light_deg"],
+            "pull_chunk": r["pull_chunk"], "pull_vector": r["pull_vector"], "from_cache": bool(r["from_cache"]),
+            "tune_s": round(time.perf_counter() - t0, 2),
+            "objective_ms_default": round(r["default_ms"], 3), "objective_ms_chosen": round(r["best_ms"], 3)}
+
+
 def gpu_arm(args, dist):
     import geminigraph_gb300 as gg
     w = WORKLOADS[args.workload]
@@ -358,6 +374,7 @@ def gpu_arm(args, dist):
     t0 = time.perf_counter()
     g = make_graph(gg, w, device)
     build_s = time.perf_counter() - t0
+    bins = tune_bins(g, args)
     info = g.info()
     V = info["vertices"]
     n = args.warmup + args.steps
@@ -428,7 +445,7 @@ def gpu_arm(args, dist):
         "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"],
                    "l2": "inputs larger than L2 (graph %.1f GB)" % (info["device_bytes"] / 1e9),
                    "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
-                   "active_edges_per_step": edges // max(len(stats), 1)},
+                   "active_edges_per_step": edges // max(len(stats), 1), "bins": bins},
         "e2e": {"value": round(e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e_max * 1000 / args.steps, 3)},
         "roofline": roofline,
@@ -460,6 +477,7 @@ def gpu_arm_batched(args, dist):
     t0 = time.perf_counter()
     g = make_graph(gg, w, device)
     build_s = time.perf_counter() - t0
+    bins = tune_bins(g, args)
     info = g.info()
     V = info["vertices"]
     bfs = args.workload == "bfs_batched"
@@ -517,7 +535,7 @@ def gpu_arm_batched(args, dist):
         "data": "synthetic (seeded R-MAT generated on the device)",
         "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"], "lanes": lanes,
                    "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
-                   "l2": "inputs larger than L2"},
+                   "l2": "inputs larger than L2", "bins": bins},
         "plain": {"value": round(plain_qps, 1), "unit": "queries/s",
                   "what": f"{len(plain_roots)} roots one at a time through the single-root kernels (device time)"},
         "speedup_vs_plain": round(value / plain_qps, 2),
@@ -554,6 +572,7 @@ def gpu_arm_serve(args, dist):
     t0 = time.perf_counter()
     graphs = [gg.Graph.generate(gg.RMAT, sc, 16, SEED + i, weighted=True, device=device) for i, sc in enumerate(scales)]
     build_s = time.perf_counter() - t0
+    bins = [tune_bins(g, args) for g in graphs]
     degs = [g.out_degree() for g in graphs]
     n = args.queries
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
@@ -625,7 +644,8 @@ def gpu_arm_serve(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 lane masks / f32",
         "data": "synthetic (seeded R-MAT generated on the device; Poisson query stream)",
         "config": {"workload": WORKLOADS["serve"]["desc"], "queries": n, "rate_qps": args.rate,
-                   "graph_build_s": round(build_s, 2), "parallelism": f"replicas x{args.gpus}"},
+                   "graph_build_s": round(build_s, 2), "parallelism": f"replicas x{args.gpus}",
+                   "bins": [{k: b[k] for k in ("source", "light_deg", "pull_chunk", "pull_vector")} for b in bins]},
         "latency_ms": {"p50": round(pct(lat, 50), 3), "p99": round(pct(lat, 99), 3)},
         "plain": {"value": round(plain_qps, 1) if plain_qps else None, "unit": "queries/s",
                   "latency_ms": {"p50": round(pct(plain_lat, 50), 3), "p99": round(pct(plain_lat, 99), 3)},
@@ -692,6 +712,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bfs", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--bins", default="autotune", choices=["autotune", "default"],
+                    help="degree bins: the autotuner's pick for this graph, or the library defaults")
     ap.add_argument("--scale", type=int, default=None, help="override the workload's R-MAT scale / grid side")
     ap.add_argument("--queries", type=int, default=2000, help="serve: queries in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: mean arrival rate (queries/s)")

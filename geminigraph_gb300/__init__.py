@@ -88,9 +88,9 @@ def library():
         "gg_server_stats_get": ([vp, ctypes.POINTER(_ServerStats)], i32),
         "gg_server_free": ([vp], i32),
         "gg_pool_bytes": ([vp, i32], u64),
-        "gg_graph_set_bins": ([vp, u32, u32], i32),
+        "gg_graph_set_bins": ([vp, u32, u32, u32], i32),
         "gg_graph_set_pr_layout": ([vp, i32], i32),
-        "gg_autotune": ([vp, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
+        "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
     for name, (args, res) in sig.items():
@@ -124,7 +124,8 @@ class _ServerStats(ctypes.Structure):
 
 
 class _TuneResult(ctypes.Structure):
-    _fields_ = [("light_deg", ctypes.c_uint32), ("pull_chunk", ctypes.c_uint32), ("best_ms", ctypes.c_double),
+    _fields_ = [("light_deg", ctypes.c_uint32), ("pull_chunk", ctypes.c_uint32), ("pull_vector", ctypes.c_uint32),
+                ("best_ms", ctypes.c_double),
                 ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32)]
 
 
@@ -277,15 +278,19 @@ class Graph:
     def edges(self):
         return self.info()["edges"]
 
-    def set_bins(self, light_deg, pull_chunk):
-        _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk))
+    def set_bins(self, light_deg, pull_chunk, pull_vector=1):
+        _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk, 1 if pull_vector else 0))
 
     def set_pr_layout(self, hot_sources):
         _check(library().gg_graph_set_pr_layout(self.h, 1 if hot_sources else 0))
 
-    def autotune(self, cache_dir=None):
+    def autotune(self, cache_dir=None, objective=("pagerank", "bfs")):
+        """Times the bin candidates on this graph for the named workloads
+        ("pagerank", "bfs", "batched") and keeps the fastest; cached on disk."""
+        mask = (1 if "pagerank" in objective else 0) | (2 if "bfs" in objective else 0) | \
+            (4 if "batched" in objective else 0)
         r = _TuneResult()
-        _check(library().gg_autotune(self.h, os.fsencode(cache_dir) if cache_dir else None, ctypes.byref(r)))
+        _check(library().gg_autotune(self.h, mask, os.fsencode(cache_dir) if cache_dir else None, ctypes.byref(r)))
         return {k: getattr(r, k) for k, _ in _TuneResult._fields_}
 
     def transpose(self):

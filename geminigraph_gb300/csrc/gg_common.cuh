@@ -58,6 +58,7 @@ constexpr uint32_t PULL_CHUNK = 256;   // default reduction-pull chunk (Dir.chun
 struct Dir {
   uint32_t light = LIGHT_DEG;       // lists up to this long are "light" (one lane)
   uint32_t chunk = PULL_CHUNK;      // edges per warp work item of the reduction pulls
+  uint32_t vec = 1;                 // chunked pulls: 1 = 16-byte window per lane, 0 = lane-strided entries
   uint64_t *off = nullptr;
   uint32_t *nbr = nullptr;
   float *w = nullptr;
@@ -246,33 +247,11 @@ __device__ __forceinline__ void big_range(const Dir &d, uint32_t c, uint32_t chu
   *e = e0 < *lo + chunk ? e0 : *lo + chunk;
 }
 
-// L2 eviction hints.  Adjacency streams through once per sweep and is loaded
-// evict-first (and not kept in L1); vertex state gathered at random is loaded
-// evict-last so that the hot (high out-degree) sources stay in L2 while the
-// adjacency streams past them.
-__device__ __forceinline__ uint64_t l2_policy_first() {
-  uint64_t p;
-  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_last() {
-  uint64_t p;
-  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint32_t ld_stream_u32(const uint32_t *p, uint64_t pol) {
+// Adjacency entries that a warp reads once (coalesced) are not kept in L1,
+// which then holds the gathered vertex state.
+__device__ __forceinline__ uint32_t ld_once(const uint32_t *p) {
   uint32_t v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ float ld_keep_f32(const float *p, uint64_t pol) {
-  float v;
-  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double ld_keep_f64(const double *p, uint64_t pol) {
-  double v;
-  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
   return v;
 }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }

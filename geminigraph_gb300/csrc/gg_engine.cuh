@@ -168,15 +168,15 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 // ---------------------------------------------------------------- pull
 // Dense mode (core/graph.hpp:1664-1855), reduction form.  For each vertex v
 // with op.want(v): acc = op.identity(v) combined (op.combine) with
-// op.gather(d, k, u) (u = the k-th entry) over its in-list, then op.finish(v, acc, deg, tally)
-// applies the slot and returns whether v is activated.  Op::Acc is the
-// message type; op.identity_coop() is the neutral element of combine.
-// Work is split by the direction's degree bins:
+// op.gather(d, k, u) (u = the k-th entry) over its in-list, then
+// op.finish(v, acc, deg, tally) applies the slot and returns whether v is
+// activated.  Op::Acc is the message type; op.identity_coop() is the
+// neutral element of combine.  Work is split by the direction's degree bins:
 //   pull_light   one warp per 32 consecutive vertices, each lane serially
-//                over a list of <= LIGHT_DEG entries (and every deg-0 vertex);
+//                over a list of <= d.light entries (and every deg-0 vertex);
 //                the warp owns the bitmap word of its 32 vertices
 //   pull_chunks / pull_big_finish
-//                every longer list cut into PULL_CHUNK-edge chunks, one warp
+//                every longer list cut into d.chunk-edge chunks, one warp
 //                per chunk, then one lane per vertex combining its chunks in
 //                order
 // The chunk kernels run after pull_light in the same stream and set their
@@ -217,11 +217,15 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
 }
 
 // Lists longer than d.light: one warp per d.chunk-edge aligned block of the
-// adjacency (d.chunk = 32 * PER_LANE, 128 / 256 / 512).  Lane l loads the
-// block's 16-byte windows l, l + 32, ... with one vector load each and
-// gathers the entries that belong to the list; partials[c] = the chunk's
-// combine (lane order, then the warp tree).
-template <class Op, int PER_LANE>
+// adjacency (d.chunk = 32 * PER_LANE, 128 / 256 / 512), PER_LANE gathers in
+// flight per lane; partials[c] = the chunk's combine (lane order, then the
+// warp tree).  Two load shapes (d.vec, picked per graph by the autotuner):
+//   VEC    lane l loads the block's 16-byte windows l, l + 32, ... with one
+//          vector load each (fewer load instructions);
+//   !VEC   lane l takes entries l, l + 32, ... (a warp's gathers touch
+//          consecutive entries, which share cache sectors where an in-list
+//          holds runs of consecutive source numbers), read past L1.
+template <class Op, int PER_LANE, bool VEC>
 __global__ void __launch_bounds__(PULL_THREADS)
     pull_chunks(Dir d, Op op, typename Op::Acc *__restrict__ partials) {
   using Acc = typename Op::Acc;
@@ -234,20 +238,34 @@ __global__ void __launch_bounds__(PULL_THREADS)
     big_range(d, (uint32_t)c, 32 * PER_LANE, &v, &lo, &b, &e);
     Acc part = op.identity_coop();
     if (op.want(v)) {
-      uint4 w[WIN];
-#pragma unroll
-      for (int i = 0; i < WIN; i++) {
-        const unsigned long long p = lo + 4 * (lane + 32 * i);
-        w[i] = p < e && p + 4 > b ? __ldg(reinterpret_cast<const uint4 *>(d.nbr + p)) : make_uint4(0, 0, 0, 0);
-      }
       Acc vals[PER_LANE];
+      if constexpr (VEC) {
+        uint4 w[WIN];
 #pragma unroll
-      for (int i = 0; i < WIN; i++) {
-        const unsigned long long p = lo + 4 * (lane + 32 * i);
-        const uint32_t u[4] = {w[i].x, w[i].y, w[i].z, w[i].w};
+        for (int i = 0; i < WIN; i++) {
+          const unsigned long long p = lo + 4 * (lane + 32 * i);
+          w[i] = p < e && p + 4 > b ? __ldg(reinterpret_cast<const uint4 *>(d.nbr + p)) : make_uint4(0, 0, 0, 0);
+        }
 #pragma unroll
-        for (int j = 0; j < 4; j++)
-          vals[4 * i + j] = p + j >= b && p + j < e ? op.gather(d, p + j, u[j]) : op.identity_coop();
+        for (int i = 0; i < WIN; i++) {
+          const unsigned long long p = lo + 4 * (lane + 32 * i);
+          const uint32_t u[4] = {w[i].x, w[i].y, w[i].z, w[i].w};
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            vals[4 * i + j] = p + j >= b && p + j < e ? op.gather(d, p + j, u[j]) : op.identity_coop();
+        }
+      } else {
+        uint32_t u[PER_LANE];
+#pragma unroll
+        for (int j = 0; j < PER_LANE; j++) {
+          const unsigned long long k = b + lane + 32 * j;
+          u[j] = k < e ? ld_once(d.nbr + k) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < PER_LANE; j++) {
+          const unsigned long long k = b + lane + 32 * j;
+          vals[j] = k < e ? op.gather(d, k, u[j]) : op.identity_coop();
+        }
       }
 #pragma unroll
       for (int j = 0; j < PER_LANE; j++) part = op.combine(part, vals[j]);
@@ -706,12 +724,21 @@ struct Launch {
       typename Op::Acc *part = nullptr;
       GG_TRY(ws(g, WS_PARTIAL, d.nbigchunks, &part));
       const unsigned cg = grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, 8);
-      if (d.chunk == 128)
-        pull_chunks<Op, 4><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
-      else if (d.chunk == 512)
-        pull_chunks<Op, 16><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
-      else
-        pull_chunks<Op, 8><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+      if (d.vec) {
+        if (d.chunk == 128)
+          pull_chunks<Op, 4, true><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+        else if (d.chunk == 512)
+          pull_chunks<Op, 16, true><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+        else
+          pull_chunks<Op, 8, true><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+      } else {
+        if (d.chunk == 128)
+          pull_chunks<Op, 4, false><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+        else if (d.chunk == 512)
+          pull_chunks<Op, 16, false><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+        else
+          pull_chunks<Op, 8, false><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
+      }
       pull_big_finish<Op><<<grid_for(d.nbig, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, op, part, act,
                                                                                                   ctr);
       launches += 2;

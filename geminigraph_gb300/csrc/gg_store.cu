@@ -465,11 +465,13 @@ static void free_bins(gg_graph *g, Dir *d) {
 
 // Rebuilds both directions' degree bins for a light-list bound and a pull
 // chunk size (the autotuner's two knobs).
-int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk) {
-  if (light < 1 || light > HEAVY_DEG || (chunk != 128 && chunk != 256 && chunk != 512)) {
-    set_error("light list bound must be 1..%u and the pull chunk 128, 256 or 512", HEAVY_DEG);
+int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk, uint32_t vec) {
+  if (light < 1 || light > HEAVY_DEG || (chunk != 128 && chunk != 256 && chunk != 512) || vec > 1) {
+    set_error("light list bound must be 1..%u, the pull chunk 128, 256 or 512 and the vector flag 0 or 1",
+              HEAVY_DEG);
     return GG_ERR_INVALID;
   }
+  g->out.vec = g->in.vec = g->pr.vec = vec;
   GG_CUDA(cudaSetDevice(g->device));
   GG_CUDA(cudaStreamSynchronize(g->stream));
   const bool alias = g->in.nbr == g->out.nbr;
@@ -660,6 +662,7 @@ int pr_layout_build(gg_graph *g) {
     g->pr = Dir();
     g->pr.light = g->in.light;
     g->pr.chunk = g->in.chunk;
+    g->pr.vec = g->in.vec;
     status = build_dir(g, k0, nullptr, k1, nullptr, n, bits, &g->pr, false);
   }
   cudaStreamSynchronize(g->stream);

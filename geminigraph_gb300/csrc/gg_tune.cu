@@ -1,9 +1,12 @@
 // Autotuner for the degree bins: the light-list bound (lists up to it get one
-// lane) and the reduction-pull chunk (edges per warp work item).  The best
-// pair depends on the graph's degree distribution, so it is measured on the
-// graph itself: every candidate rebuilds the bins and times two float
-// PageRank iterations (light and chunked pulls) plus one BFS from the vertex
-// of largest out-degree (push, pull, small runs) with CUDA events; the
+// lane), the reduction-pull chunk (edges per warp work item) and the chunk
+// load shape (16-byte windows per lane or lane-strided entries).  The best
+// choice depends on the graph's degree distribution, so it is measured on the
+// graph itself: every candidate rebuilds the bins and times, with CUDA
+// events, the objective's workloads: two float PageRank iterations (light
+// and chunked pulls), one BFS from the vertex of largest out-degree (push,
+// pull, small runs) and one 64-root batched BFS (and SSSP on a weighted
+// graph); the
 // fastest is kept and recorded in a cache file keyed by a fingerprint of the
 // graph, so the next load of the same graph skips the search.
 #include <stdio.h>
@@ -18,7 +21,7 @@
 
 namespace gg {
 
-int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk);
+int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk, uint32_t vec);
 
 __global__ void degree_fingerprint(const uint32_t *__restrict__ out_deg, const uint32_t *__restrict__ in_deg,
                                    uint32_t V, unsigned long long *out, unsigned *argmax_deg) {
@@ -49,7 +52,7 @@ static std::string cache_file(const char *dir) {
   } else {
     d = "/tmp/geminigraph_gb300";
   }
-  return d + "/bins_v1.txt";
+  return d + "/bins_v2.txt";
 }
 
 static void mkdirs(const std::string &path) {
@@ -63,17 +66,21 @@ using namespace gg;
 
 extern "C" {
 
-int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk) {
+int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint32_t pull_vector) {
   if (!g) {
     set_error("null graph");
     return GG_ERR_INVALID;
   }
-  return rebuild_bins(g, light_deg, pull_chunk);
+  return rebuild_bins(g, light_deg, pull_chunk, pull_vector);
 }
 
-int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out) {
+int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_result *out) {
   if (!g) {
     set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  if (objective == 0 || (objective & ~(uint32_t)(GG_TUNE_PAGERANK | GG_TUNE_BFS | GG_TUNE_BATCHED))) {
+    set_error("objective must be a non-empty mask of GG_TUNE_PAGERANK, GG_TUNE_BFS and GG_TUNE_BATCHED");
     return GG_ERR_INVALID;
   }
   GG_CUDA(cudaSetDevice(g->device));
@@ -98,30 +105,45 @@ int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out) {
   cudaFree(d_h);
   const uint32_t root = hm[1] < g->V ? hm[1] : 0;
   char key[160];
-  snprintf(key, sizeof(key), "%u:%llu:%llu:%d:%d:%016llx", g->V, (unsigned long long)g->E,
-           (unsigned long long)g->nadj, g->weighted, g->symmetric, h);
+  snprintf(key, sizeof(key), "%u:%llu:%llu:%d:%d:%u:%016llx", g->V, (unsigned long long)g->E,
+           (unsigned long long)g->nadj, g->weighted, g->symmetric, objective, h);
   gg_tune_result r;
   memset(&r, 0, sizeof(r));
   // cached?
   const std::string file = cache_file(cache_dir);
   if (FILE *f = fopen(file.c_str(), "r")) {
     char k[160];
-    unsigned light, chunk;
+    unsigned light, chunk, vec;
     double ms;
-    while (fscanf(f, "%159s %u %u %lf", k, &light, &chunk, &ms) == 4) {
+    while (fscanf(f, "%159s %u %u %u %lf", k, &light, &chunk, &vec, &ms) == 5) {
       if (std::string(k) == key) {
         r.light_deg = light;
         r.pull_chunk = chunk;
+        r.pull_vector = vec;
         r.best_ms = ms;
         r.from_cache = 1;
       }
     }
     fclose(f);
     if (r.from_cache) {
-      GG_TRY(rebuild_bins(g, r.light_deg, r.pull_chunk));
+      GG_TRY(rebuild_bins(g, r.light_deg, r.pull_chunk, r.pull_vector));
       if (out) *out = r;
       return GG_OK;
     }
+  }
+  // 64 roots of nonzero out-degree for the batched objective (a fixed
+  // multiplicative stream over the vertices)
+  std::vector<uint32_t> roots;
+  if (objective & GG_TUNE_BATCHED) {
+    std::vector<uint32_t> od(g->V);
+    GG_CUDA(cudaMemcpy(od.data(), g->out.deg, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost));
+    uint64_t x = 0x2545F4914F6CDD1Dull;
+    for (uint32_t tries = 0; roots.size() < 64 && tries < 64u * 1024u; tries++) {
+      x = x * 6364136223846793005ull + 1442695040888963407ull;
+      const uint32_t v = (uint32_t)((x >> 32) % g->V);
+      if (od[v]) roots.push_back(v);
+    }
+    if (roots.empty()) roots.push_back(root);
   }
   const uint32_t lights[] = {16, 32, 64};
   const uint32_t chunks[] = {128, 256, 512};
@@ -129,37 +151,52 @@ int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out) {
     gg_run_stats st;
     memset(&st, 0, sizeof(st));
     double t = 0;
-    GG_TRY(gg_pagerank_f32(g, 2, nullptr, nullptr, &st));
-    t += st.device_ms;
-    GG_TRY(gg_bfs(g, root, nullptr, &st));
-    t += st.device_ms;
+    if (objective & GG_TUNE_PAGERANK) {
+      GG_TRY(gg_pagerank_f32(g, 2, nullptr, nullptr, &st));
+      t += st.device_ms;
+    }
+    if (objective & GG_TUNE_BFS) {
+      GG_TRY(gg_bfs(g, root, nullptr, &st));
+      t += st.device_ms;
+    }
+    if (objective & GG_TUNE_BATCHED) {
+      GG_TRY(gg_bfs_batched(g, roots.data(), (int)roots.size(), nullptr, nullptr, nullptr, nullptr, &st));
+      t += st.device_ms;
+      if (g->weighted) {
+        GG_TRY(gg_sssp_batched(g, roots.data(), (int)roots.size(), nullptr, nullptr, &st));
+        t += st.device_ms;
+      }
+    }
     *ms = t;
     return GG_OK;
   };
   double best = 1e300, def = 0;
-  uint32_t bl = LIGHT_DEG, bc = PULL_CHUNK;
+  uint32_t bl = LIGHT_DEG, bc = PULL_CHUNK, bv = 1;
   for (uint32_t light : lights)
-    for (uint32_t chunk : chunks) {
-      GG_TRY(rebuild_bins(g, light, chunk));
-      double ms0, ms1;
-      GG_TRY(measure(&ms0));  // warm
-      GG_TRY(measure(&ms1));
-      r.candidates += 1;
-      if (light == LIGHT_DEG && chunk == PULL_CHUNK) def = ms1;
-      if (ms1 < best) {
-        best = ms1;
-        bl = light;
-        bc = chunk;
+    for (uint32_t chunk : chunks)
+      for (uint32_t vec = 0; vec < 2; vec++) {
+        GG_TRY(rebuild_bins(g, light, chunk, vec));
+        double ms0, ms1;
+        GG_TRY(measure(&ms0));  // warm
+        GG_TRY(measure(&ms1));
+        r.candidates += 1;
+        if (light == LIGHT_DEG && chunk == PULL_CHUNK && vec == 1) def = ms1;
+        if (ms1 < best) {
+          best = ms1;
+          bl = light;
+          bc = chunk;
+          bv = vec;
+        }
       }
-    }
-  GG_TRY(rebuild_bins(g, bl, bc));
+  GG_TRY(rebuild_bins(g, bl, bc, bv));
   r.light_deg = bl;
   r.pull_chunk = bc;
+  r.pull_vector = bv;
   r.best_ms = best;
   r.default_ms = def;
   mkdirs(file);
   if (FILE *f = fopen(file.c_str(), "a")) {
-    fprintf(f, "%s %u %u %.6f\n", key, bl, bc, best);
+    fprintf(f, "%s %u %u %u %.6f\n", key, bl, bc, bv, best);
     fclose(f);
   }
   if (out) *out = r;

@@ -216,24 +216,35 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
 /* ---- autotuner (no counterpart in the reference; Graph::tune_chunks,
  * core/graph.hpp:1341-1404, balances threads by edge counts at load) ----
  * The pull kernels split vertices into light lists (<= light_deg entries, one
- * lane each) and longer lists cut into pull_chunk-edge warp work items.
- * gg_graph_set_bins sets both (light_deg 1..2048; pull_chunk 128, 256 or 512);
- * gg_autotune times 9 candidate pairs on the graph itself (two float PageRank
- * iterations and one BFS per candidate, CUDA events), keeps the fastest and
- * records it in <cache_dir>/bins_v1.txt (cache_dir NULL: $GG_TUNE_CACHE, else
- * ~/.cache/geminigraph_gb300) under a fingerprint of the graph; a later call on
- * the same graph reads the cache instead of searching.  Results of every
- * toolkit are independent of the bins. */
+ * lane each) and longer lists cut into pull_chunk-edge warp work items, whose
+ * lanes load 16-byte windows of the list (pull_vector = 1) or every 32nd
+ * entry (0).  gg_graph_set_bins sets all three (light_deg 1..2048;
+ * pull_chunk 128, 256 or 512; pull_vector 0 or 1).  gg_autotune times the
+ * 18 candidates on the graph itself with CUDA events, on the workloads the
+ * objective mask names (GG_TUNE_PAGERANK: two float PageRank iterations;
+ * GG_TUNE_BFS: one BFS; GG_TUNE_BATCHED: one 64-root gg_bfs_batched, and
+ * gg_sssp_batched on a weighted graph), keeps the fastest and records it in
+ * <cache_dir>/bins_v2.txt (cache_dir NULL: $GG_TUNE_CACHE, else
+ * ~/.cache/geminigraph_gb300) under a fingerprint of the graph and the
+ * objective; a later call on the same graph reads the cache instead of
+ * searching.  Traversal results (BFS, CC, SSSP) do not depend on the bins;
+ * PageRank and BC sums may differ in the last bits. */
 typedef struct {
   uint32_t light_deg;
   uint32_t pull_chunk;
-  double best_ms;        /* timing workload with the chosen pair */
-  double default_ms;     /* the same with the defaults (32, 256) */
-  int32_t candidates;    /* pairs timed (0 when read from the cache) */
+  uint32_t pull_vector;
+  double best_ms;        /* timing workload with the chosen bins */
+  double default_ms;     /* the same with the defaults (32, 256, 1) */
+  int32_t candidates;    /* candidates timed (0 when read from the cache) */
   int32_t from_cache;
 } gg_tune_result;
 
-int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk);
+int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint32_t pull_vector);
+
+#define GG_TUNE_PAGERANK 1u
+#define GG_TUNE_BFS 2u
+#define GG_TUNE_BATCHED 4u
+int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_result *out);
 
 /* PageRank's adjacency layout (no reference counterpart; the reference pulls
  * its CSC as loaded).  hot_sources = 1 (the default): on its first call
@@ -245,7 +256,6 @@ int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk);
  * 0 frees the copy and pulls the plain incoming adjacency.  The copy is
  * dropped by gg_graph_transpose and counted in device_bytes. */
 int gg_graph_set_pr_layout(gg_graph *g, int hot_sources);
-int gg_autotune(gg_graph *g, const char *cache_dir, gg_tune_result *out);
 
 /* ---- engine primitives ---- */
 

@@ -333,11 +333,11 @@ def test_pull_bins_cover_all_degrees():
     assert np.array_equal(lab, olab)
 
 
-@pytest.mark.parametrize("light,chunk", [(16, 128), (64, 512), (1, 256)])
-def test_results_do_not_depend_on_bins(light, chunk):
+@pytest.mark.parametrize("light,chunk,vec", [(16, 128, 1), (64, 512, 0), (1, 256, 0), (32, 256, 0)])
+def test_results_do_not_depend_on_bins(light, chunk, vec):
     V, s, d, w, root = case("rmat16")
     g = gg.Graph.from_edges(V, s, d, w)
-    g.set_bins(light, chunk)
+    g.set_bins(light, chunk, vec)
     o = OracleGraph(V, s, d, w)
     parent, st = g.bfs(root)
     op, otr = o.bfs(root)
@@ -353,7 +353,7 @@ def test_results_do_not_depend_on_bins(light, chunk):
     lv, _, _, _, _ = gg.bfs_batched(g, [root, 0, 5])
     assert np.array_equal(lv[0], bfs_levels(op, root))
     gs = gg.Graph.from_edges(V, s, d, symmetric=True)
-    gs.set_bins(light, chunk)
+    gs.set_bins(light, chunk, vec)
     assert np.array_equal(gs.cc()[0], OracleGraph(V, s, d, symmetric=True).cc()[0])
 
 
@@ -361,12 +361,13 @@ def test_autotune_picks_and_caches(tmp_path):
     V, s, d, w, root = case("rmat16")
     g = gg.Graph.from_edges(V, s, d, w)
     r1 = g.autotune(str(tmp_path))
-    assert r1["candidates"] == 9 and r1["from_cache"] == 0
+    assert r1["candidates"] == 18 and r1["from_cache"] == 0
     assert r1["light_deg"] in (16, 32, 64) and r1["pull_chunk"] in (128, 256, 512)
     assert r1["best_ms"] <= r1["default_ms"]
     g2 = gg.Graph.from_edges(V, s, d, w)
     r2 = g2.autotune(str(tmp_path))
-    assert r2["from_cache"] == 1 and (r2["light_deg"], r2["pull_chunk"]) == (r1["light_deg"], r1["pull_chunk"])
+    key = ("light_deg", "pull_chunk", "pull_vector")
+    assert r2["from_cache"] == 1 and [r2[k] for k in key] == [r1[k] for k in key]
     parent, st = g2.bfs(root)
     assert st.rows() == OracleGraph(V, s, d).bfs(root)[1]
     with pytest.raises(gg.GeminiError):
@@ -398,3 +399,19 @@ def test_pagerank_layouts_agree(name):
     g.transpose()
     again, _, _ = g.pagerank(20)
     assert np.array_equal(again, hot)
+
+
+def test_autotune_objectives(tmp_path):
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d, w)
+    seen = set()
+    for obj in (("pagerank",), ("bfs",), ("batched",)):
+        r = g.autotune(str(tmp_path), objective=obj)
+        assert r["candidates"] == 18 and r["from_cache"] == 0 and r["best_ms"] > 0
+        seen.add(obj)
+    assert g.autotune(str(tmp_path), objective=("batched",))["from_cache"] == 1
+    lv, _, _, _, _ = gg.bfs_batched(g, [root, 1, 2])
+    o = OracleGraph(V, s, d, w)
+    assert np.array_equal(lv[0], bfs_levels(o.bfs(root)[0], root))
+    with pytest.raises(gg.GeminiError):
+        g.autotune(str(tmp_path), objective=())

@@ -94,9 +94,36 @@ def build_toolkits(verbose=False):
     return BIN
 
 
+EXAMPLES = ("engine_toolkits",)
+
+
+def build_examples(verbose=False):
+    """Programs written against the header-only engine (gemini/engine.cuh):
+    nvcc with extended lambdas, linked to libgemini_gb300.so."""
+    os.makedirs(BIN, exist_ok=True)
+    headers = glob.glob(os.path.join(CPP, "*", "*.hpp")) + glob.glob(os.path.join(CPP, "*", "*.cuh")) + \
+        glob.glob(os.path.join(INCLUDE, "*.h"))
+    for ex in EXAMPLES:
+        src = os.path.join(CPP, "examples", ex + ".cu")
+        out = os.path.join(BIN, ex)
+        if not _stale(out, [src, LIB] + headers):
+            continue
+        cmd = [_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-I", INCLUDE, "-I", CPP,
+                                  src, "-o", out, "-L", PKG, "-lgemini_gb300", "-Xlinker", "-rpath,$ORIGIN/.."]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + p.stdout + p.stderr)
+    return BIN
+
+
 def build(verbose=False):
     lib = build_library(verbose)
-    build_toolkits(verbose)
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        jobs = [ex.submit(build_toolkits, verbose), ex.submit(build_examples, verbose)]
+        for j in jobs:
+            j.result()
     return lib
 
 

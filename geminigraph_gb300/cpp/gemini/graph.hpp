@@ -7,9 +7,11 @@
 // Differences from the reference, by design:
 //  * one partition on one GPU: partition_id is 0, partitions is 1, and
 //    gather_vertex_array is a no-op;
-//  * the five toolkits' process_edges/process_vertices loops run on the GPU
-//    inside the library (bfs(), pagerank(), cc(), sssp(), bc() below); a
-//    std::function lambda cannot run on the device;
+//  * the five toolkits run on the GPU inside the library (bfs(), pagerank(),
+//    cc(), sssp(), bc() below); a std::function lambda cannot run on the
+//    device, so user-written process_edges / process_vertices loops use the
+//    device-lambda engine of gemini/engine.cuh (compiled with nvcc) on the
+//    same Graph;
 //  * errors throw gemini::Error instead of assert()/exit(-1).
 #ifndef GEMINI_GB300_GRAPH_HPP
 #define GEMINI_GB300_GRAPH_HPP

@@ -1055,6 +1055,23 @@ int gg_graph_transpose(gg_graph *g) {
   return GG_OK;
 }
 
+int gg_graph_device_view(const gg_graph *g, int incoming, gg_device_adj *out) {
+  if (!g || !out) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  const Dir &d = incoming ? g->in : g->out;
+  out->offsets = d.off;
+  out->neighbours = d.nbr;
+  out->weights = d.w;
+  out->degree = d.deg;
+  out->vertices = g->V;
+  out->entries = g->nadj;
+  out->edges = g->E;
+  out->device = g->device;
+  return GG_OK;
+}
+
 int gg_graph_adjacency(const gg_graph *g, int incoming, uint64_t *offsets, uint32_t *neighbours, float *weights,
                        uint32_t *degree) {
   if (!g) {

@@ -115,6 +115,25 @@ int gg_graph_transpose(gg_graph *g);
 int gg_graph_adjacency(const gg_graph *g, int incoming, uint64_t *offsets, uint32_t *neighbours,
                        float *weights, uint32_t *degree);
 
+/* Device view of one direction of the graph, for kernels compiled outside
+ * the library (the process_edges / process_vertices templates of
+ * gemini/engine.cuh).  Plain device pointers owned by the graph, valid until
+ * gg_graph_free; incoming = 1 gives the CSC (in-lists), 0 the CSR, as
+ * swapped by gg_graph_transpose.  Replaces the reference's direct access to
+ * the partition's adjacency (outgoing_adj_*, incoming_adj_*,
+ * core/graph.hpp:121-140). */
+typedef struct {
+  const uint64_t *offsets;     /* vertices + 1 */
+  const uint32_t *neighbours;  /* entries */
+  const float *weights;        /* entries; NULL when unweighted */
+  const uint32_t *degree;      /* vertices */
+  uint32_t vertices;
+  uint64_t entries;
+  uint64_t edges;              /* edge records: the |E| of the sparse/dense switch */
+  int32_t device;
+} gg_device_adj;
+int gg_graph_device_view(const gg_graph *g, int incoming, gg_device_adj *out);
+
 /* ---- toolkits (the compute() of toolkits/*.cpp, on one GPU) ----
  * Output pointers are host memory; NULL leaves the result on the device
  * (see gg_result_device_ptr).  stats may be NULL. */

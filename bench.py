@@ -66,12 +66,15 @@ WORKLOADS = {
                   desc="serving: 4 resident weighted R-MAT graphs (scales 20, 22, 24, 26, edge factor 16), Poisson "
                        "arrivals at 5000 queries/s, graph drawn with p = 0.4/0.3/0.2/0.1, 75% BFS / 25% SSSP, "
                        "seeded uniform non-isolated roots"),
+    "bc_batched": dict(kind="rmat", scale=24, ef=16, weighted=False, symmetric=False,
+                       desc="batched BC (double), 64 seeded roots per launch, on directed R-MAT scale 24, "
+                            "edge factor 16"),
     "sssp_batched": dict(kind="rmat", scale=24, ef=16, weighted=True, symmetric=False,
                          desc="batched SSSP, 64 seeded roots per launch, on R-MAT scale 24, edge factor 16, "
                               "float weights in [0,1)"),
 }
 REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "pagerank_f64": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs",
-           "bfs_batched": "bfs", "sssp_batched": "sssp", "serve": "bfs"}
+           "bfs_batched": "bfs", "sssp_batched": "sssp", "bc_batched": "bc", "serve": "bfs"}
 
 
 def log(*a):
@@ -244,7 +247,7 @@ def step_args(gg, g, workload, count):
 # ----------------------------------------------------------------- CPU side
 def ref_sample_scale(workload):
     return {"bfs": 22, "cc": 21, "pagerank": 20, "pagerank_f64": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024, "bfs_batched": 22,
-            "sssp_batched": 21, "serve": 22}[workload]
+            "sssp_batched": 21, "bc_batched": 21, "serve": 22}[workload]
 
 
 def cpu_reference(gg, workload, nsteps, warmup):
@@ -266,7 +269,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
     src, dst = words[:, 0].copy(), words[:, 1].copy()
     wts = words[:, 2].view(np.float32).copy() if w["weighted"] else None
     n = warmup + nsteps
-    if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched", "serve"):
+    if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched", "bc_batched", "serve"):
         args = gg.pick_roots(np.bincount(src, minlength=V), n, seed=SEED + 2000)
     elif workload == "bfs_grid":
         args = [0] * n
@@ -282,7 +285,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
             tr = og.bfs(a)[1]
         elif workload in ("sssp", "sssp_batched"):
             tr = og.sssp(a)[1]
-        elif workload == "bc":
+        elif workload in ("bc", "bc_batched"):
             tr = og.bc(a)[2]
         elif workload in ("pagerank", "pagerank_f64"):
             tr = og.pagerank(a)[2]
@@ -317,7 +320,7 @@ def cpu_reference(gg, workload, nsteps, warmup):
             og.bfs(a)
         elif workload in ("sssp", "sssp_batched"):
             og.sssp(a)
-        elif workload == "bc":
+        elif workload in ("bc", "bc_batched"):
             og.bc(a)
         elif workload in ("pagerank", "pagerank_f64"):
             og.pagerank(a)
@@ -338,14 +341,18 @@ def reference_arm(args, dist):
     import geminigraph_gb300 as gg
     w = WORKLOADS[args.workload]
     r = cpu_reference(gg, args.workload, args.steps, args.warmup)
+    if args.workload.endswith("_batched") or args.workload == "serve":
+        # the reference has no batching: its queries/s is one root at a time
+        r["value"], r["unit"] = len(r["times"]) / sum(r["times"]), "queries/s"
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(r["value"], 4), "unit": "GTEPS",
+        "impl": "reference", "metric": METRIC, "value": round(r["value"], 4), "unit": r["unit"],
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * sum(r["times"]) / len(r["times"]), 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f32", "pagerank_f64": "f64"}.get(args.workload, "u32"),
+        "scaling": "weak", "vs_baseline": None, "dtype": {"sssp": "f32", "bc": "f64", "pagerank": "f32", "pagerank_f64": "f64", "sssp_batched": "f32",
+                                                     "bc_batched": "f64"}.get(args.workload, "u32"),
         "data": "synthetic", "config": {"workload": w["desc"], "sample": r["sample"]},
         "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": round(r["value"], 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": round(r["value"], 4), "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -357,7 +364,7 @@ def tune_bins(g, args):
     if args.bins == "default":
         return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1}
     objective = ("pagerank",) if args.workload.startswith("pagerank") else \
-        ("batched",) if args.workload in ("bfs_batched", "sssp_batched", "serve") else \
+        ("batched",) if args.workload in ("bfs_batched", "sssp_batched", "bc_batched", "serve") else \
         ("bfs",) if args.workload.startswith("bfs") else ("pagerank", "bfs")
     t0 = time.perf_counter()
     r = g.autotune(objective=objective)
@@ -485,10 +492,15 @@ def gpu_arm_batched(args, dist):
     roots = gg.pick_roots(g.out_degree(), lanes * (args.warmup + 2 * args.steps), seed=SEED + 3000)
     batches = [roots[i * lanes:(i + 1) * lanes] for i in range(args.warmup + 2 * args.steps)]
 
+    bc = args.workload == "bc_batched"
+
     def run_batch(rs, host):
         if bfs:
             _, _, _, edges, st = gg.bfs_batched(g, rs, levels=host, parents=False, timing=True)
             return st, int(edges.sum())
+        if bc:
+            _, _, _, st = gg.bc_batched(g, rs, outputs=host, timing=True)
+            return st, 0
         _, _, st = gg.sssp_batched(g, rs, distances=host, timing=True)
         return st, 0
 
@@ -516,6 +528,8 @@ def gpu_arm_batched(args, dist):
     for r in plain_roots:
         if bfs:
             _, st = g.bfs(r, to_host=False)
+        elif bc:
+            _, _, st = g.bc(r, to_host=False)
         else:
             _, st = g.sssp(r, to_host=False)
         plain_ms += st.device_ms
@@ -531,7 +545,7 @@ def gpu_arm_batched(args, dist):
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_max * 1000 / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64 lane masks" if bfs else "f32",
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 lane masks" if bfs else ("f64" if bc else "f32"),
         "data": "synthetic (seeded R-MAT generated on the device)",
         "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"], "lanes": lanes,
                    "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
@@ -540,7 +554,7 @@ def gpu_arm_batched(args, dist):
                   "what": f"{len(plain_roots)} roots one at a time through the single-root kernels (device time)"},
         "speedup_vs_plain": round(value / plain_qps, 2),
         "e2e": {"value": round(dist.sum(lanes * args.steps) / e_max, 1), "unit": "queries/s",
-                "h2d_bytes_per_step": 4 * lanes, "d2h_bytes_per_step": 4 * lanes * V,
+                "h2d_bytes_per_step": 4 * lanes, "d2h_bytes_per_step": (16 if bc else 4) * lanes * V,
                 "ms_per_step": round(e_max * 1000 / args.steps, 3)},
         "gpu_launches": launches, "clocks": clk,
         "trace_first_step": [list(r) for r in first.rows(with_ms=True)[:60]] if first else [],

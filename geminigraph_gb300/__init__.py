@@ -89,6 +89,7 @@ def library():
         "gg_server_free": ([vp], i32),
         "gg_pool_bytes": ([vp, i32], u64),
         "gg_graph_set_bins": ([vp, u32, u32, u32], i32),
+        "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_pr_layout": ([vp, i32], i32),
         "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
@@ -389,6 +390,21 @@ def sssp_batched(g, roots, distances=True, timing=False):
         st.enable_call_timing()
     _check(library().gg_sssp_batched(g.h, _ptr(r), len(r), _ptr(dist), _ptr(reached), ctypes.byref(st.s)))
     return dist, reached, st
+
+
+def bc_batched(g, roots, outputs=True, timing=False):
+    """Batched BC of up to 64 roots: (dependencies (len(roots), V), 1/num_paths
+    (len(roots), V), reached, stats); the arrays are None when outputs=False."""
+    r = _roots_array(roots)
+    V = g.vertices
+    dep = np.empty((len(r), V), np.float64) if outputs else None
+    inv = np.empty((len(r), V), np.float64) if outputs else None
+    reached = np.zeros(len(r), np.uint64)
+    st = RunStats()
+    if timing:
+        st.enable_call_timing()
+    _check(library().gg_bc_batched(g.h, _ptr(r), len(r), _ptr(dep), _ptr(inv), _ptr(reached), ctypes.byref(st.s)))
+    return dep, inv, reached, st
 
 
 def result_checksum(values, kind):

@@ -175,6 +175,17 @@ int gg_bfs_batched(gg_graph *g, const uint32_t *roots, int nroots, int32_t *leve
 int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, float *distances, uint64_t *reached,
                     gg_run_stats *stats);
 
+/* Batched betweenness centrality (no reference counterpart; per lane the
+ * computation of toolkits/bc.cpp:24-196): up to 64 roots in one pass per
+ * level.  dependencies and inv_num_paths (either may be NULL) receive
+ * nroots x vertices doubles, lane-major (root i at [i * vertices]): the
+ * reference's printed dependencies and 1 / num_paths, NaN / inf where the
+ * root does not reach; reached[i] = vertices root i reaches.  Device memory:
+ * 2 x 64 x 8 bytes per vertex plus 8 bytes per vertex per BFS level.
+ * Dependencies equal the single-root gg_bc's within summation rounding. */
+int gg_bc_batched(gg_graph *g, const uint32_t *roots, int nroots, double *dependencies, double *inv_num_paths,
+                  uint64_t *reached, gg_run_stats *stats);
+
 /* Checksum of one traversal result, as the serving loop reports it: the sum
  * (mod 2^64) over reached vertices v of mix64(v * 0x9E3779B97F4A7C15 + x), where
  * x is the hop count (kind 0: int32 levels, -1 = unreached) or the float bits

@@ -77,3 +77,30 @@ def test_batched_argument_errors(case):
     gu = gg.Graph.from_edges(V, s, d)
     with pytest.raises(gg.GeminiError):
         gg.sssp_batched(gu, [0])
+
+
+@pytest.mark.parametrize("n", [1, 5, 64])
+def test_bc_batched_lanes_equal_single_runs(case, n):
+    """Every lane's dependencies and 1/num_paths equal the single-root BC
+    (gg_bc) of its root: NaN / inf in the same places, path counts exact,
+    dependencies within relative L1 1e-10 (sums in another order)."""
+    V, s, d, w, g = case
+    roots = roots_for(V, s, max(n, 3), seed=100 + n)[:n]
+    dep, inv, reached, st = gg.bc_batched(g, roots)
+    for i, r in enumerate(roots):
+        sdep, sinv, _ = g.bc(r)
+        assert np.array_equal(np.isnan(dep[i]), np.isnan(sdep)), f"lane {i} root {r}"
+        assert np.array_equal(inv[i], sinv)
+        ok = ~np.isnan(sdep)
+        den = max(np.abs(sdep[ok]).sum(), 1e-300)
+        assert np.abs(dep[i][ok] - sdep[ok]).sum() / den < 1e-10
+        assert int(reached[i]) == int(np.isfinite(sinv).sum())
+    assert st.calls >= 2
+
+
+def test_bc_batched_rejects_bad_arguments(case):
+    V, s, d, w, g = case
+    with pytest.raises(gg.GeminiError):
+        gg.bc_batched(g, [V])
+    with pytest.raises((gg.GeminiError, ValueError)):
+        gg.bc_batched(g, list(range(65)))

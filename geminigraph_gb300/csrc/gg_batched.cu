@@ -293,10 +293,13 @@ __device__ __forceinline__ u64 result_term(uint32_t v, uint32_t x) {
   return gg_mix64((u64)v * 0x9E3779B97F4A7C15ull + x);
 }
 
-// Per-lane digests of the lanes in mask: out[l] reached, out[64+l] checksum,
-// out[128+l] out-degree sum of reached vertices.  BFS: x = hop count; SSSP:
-// x = the distance's float bits.  One warp per 32 vertices; lane j of the
-// warp keeps traversal lanes j and j + 32.
+// Per-lane digests of the lanes in mask: out[l] reached, out[64+l] checksum
+// (SUM only), out[128+l] out-degree sum of reached vertices.  BFS: x = hop
+// count; SSSP: x = the distance's float bits.  A warp walks vertices one at
+// a time; thread t keeps traversal lanes t and t + 32, so the per-lane state
+// of a vertex (64 consecutive entries) is read with two coalesced loads and
+// the sums stay in registers until the end.
+template <bool SUM>
 __global__ void __launch_bounds__(256)
     lanes_digest(uint32_t V, u64 mask, const u64 *__restrict__ visit, const uint32_t *__restrict__ lvl,
                  const uint32_t *__restrict__ start, const float *__restrict__ dist,
@@ -304,49 +307,52 @@ __global__ void __launch_bounds__(256)
   __shared__ u64 s_out[3 * LANES];
   for (int i = threadIdx.x; i < 3 * LANES; i += blockDim.x) s_out[i] = 0;
   __syncthreads();
-  const unsigned lane = lane_id();
-  u64 acc[2][3] = {{0, 0, 0}, {0, 0, 0}};
-  const size_t nwarps = (size_t)gridDim.x * 8;
-  for (size_t g = (size_t)blockIdx.x * 8 + (threadIdx.x >> 5); g * 32 < V; g += nwarps) {
-    const size_t v = g * 32 + lane;
-    const bool in = v < V;
-    const uint32_t dg = in ? out_deg[v] : 0u;
-    u64 vm = 0;
-    if (visit) vm = in ? visit[v] & mask : 0ull;
-    if (visit && !__any_sync(GG_FULL, vm != 0)) continue;
-    u64 rest = mask;
-    while (rest) {
-      const int l = __ffsll((long long)rest) - 1;
-      rest &= rest - 1;
-      bool hit;
-      uint32_t x = 0;
-      if (visit) {
-        hit = (vm >> l) & 1ull;
-        if (hit) x = lvl[v * LANES + l] - start[l];
-      } else {
-        const float dv = in ? dist[v * LANES + l] : 1e9f;
-        hit = dv < 1e9f;
-        x = __float_as_uint(dv);
+  const unsigned t = lane_id();
+  const bool m0 = (mask >> t) & 1ull, m1 = (mask >> (t + 32)) & 1ull;
+  const uint32_t st0 = visit ? start[t] : 0u, st1 = visit ? start[t + 32] : 0u;
+  u64 c0 = 0, c1 = 0, h0 = 0, h1 = 0, e0 = 0, e1 = 0;
+  const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
+  for (size_t v = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < V; v += nwarps) {
+    bool hit0, hit1;
+    uint32_t x0 = 0, x1 = 0;
+    if (visit) {
+      const u64 vm = visit[v] & mask;
+      if (!vm) continue;
+      hit0 = (vm >> t) & 1ull;
+      hit1 = (vm >> (t + 32)) & 1ull;
+      if (SUM) {
+        if (hit0) x0 = lvl[v * LANES + t] - st0;
+        if (hit1) x1 = lvl[v * LANES + t + 32] - st1;
       }
-      const unsigned cnt = __popc(__ballot_sync(GG_FULL, hit));
-      const u64 h = warp_sum(hit ? result_term((uint32_t)v, x) : 0ull);
-      const unsigned lo = __reduce_add_sync(GG_FULL, hit ? (dg & 0xffffu) : 0u);
-      const unsigned hi = __reduce_add_sync(GG_FULL, hit ? (dg >> 16) : 0u);
-      if ((unsigned)(l & 31) == lane) {
-        u64 *a = acc[l >> 5];
-        a[0] += cnt;
-        a[1] += h;
-        a[2] += (u64)lo + ((u64)hi << 16);
-      }
+    } else {
+      const float d0 = dist[v * LANES + t], d1 = dist[v * LANES + t + 32];
+      hit0 = m0 && d0 < 1e9f;
+      hit1 = m1 && d1 < 1e9f;
+      x0 = __float_as_uint(d0);
+      x1 = __float_as_uint(d1);
+      if (!__any_sync(GG_FULL, hit0 || hit1)) continue;
+    }
+    const uint32_t dg = out_deg[v];
+    if (hit0) {
+      c0 += 1;
+      e0 += dg;
+      if (SUM) h0 += result_term((uint32_t)v, x0);
+    }
+    if (hit1) {
+      c1 += 1;
+      e1 += dg;
+      if (SUM) h1 += result_term((uint32_t)v, x1);
     }
   }
-  for (int half = 0; half < 2; half++) {
-    const int l = (int)lane + 32 * half;
-    if ((mask >> l) & 1ull) {
-      atomicAdd(&s_out[l], acc[half][0]);
-      atomicAdd(&s_out[LANES + l], acc[half][1]);
-      atomicAdd(&s_out[2 * LANES + l], acc[half][2]);
-    }
+  if (m0) {
+    if (c0) atomicAdd(&s_out[t], c0);
+    if (h0) atomicAdd(&s_out[LANES + t], h0);
+    if (e0) atomicAdd(&s_out[2 * LANES + t], e0);
+  }
+  if (m1) {
+    if (c1) atomicAdd(&s_out[t + 32], c1);
+    if (h1) atomicAdd(&s_out[LANES + t + 32], h1);
+    if (e1) atomicAdd(&s_out[2 * LANES + t + 32], e1);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 3 * LANES; i += blockDim.x)
@@ -725,8 +731,13 @@ int LanePool::digest(u64 mask, u64 *reached, u64 *checksum, u64 *edges) {
   const uint32_t V = g_->V;
   GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
   GG_CUDA(cudaMemsetAsync(out_dev_, 0, 3 * LANES * sizeof(u64), s_));
-  lanes_digest<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-      V, mask, kind_ == BFS ? visit_ : nullptr, lvl_, start_dev_, dist_, g_->out.deg, out_dev_);
+  const unsigned grid = grid_for((size_t)V * 32, 256, g_->num_sms, 8);
+  if (checksum)
+    lanes_digest<true><<<grid, 256, 0, s_>>>(V, mask, kind_ == BFS ? visit_ : nullptr, lvl_, start_dev_, dist_,
+                                             g_->out.deg, out_dev_);
+  else
+    lanes_digest<false><<<grid, 256, 0, s_>>>(V, mask, kind_ == BFS ? visit_ : nullptr, lvl_, start_dev_, dist_,
+                                              g_->out.deg, out_dev_);
   launches += 1;
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaMemcpyAsync(out_host_, out_dev_, 3 * LANES * sizeof(u64), cudaMemcpyDeviceToHost, s_));
@@ -810,7 +821,7 @@ static int run_batch(gg_graph *g, LanePool::Kind kind, const uint32_t *roots, in
   while (status == GG_OK && p->active()) status = p->step();
   const u64 mask = nroots == 64 ? ~0ull : ((1ull << nroots) - 1);
   u64 r[LANES], c[LANES], e[LANES];
-  if (status == GG_OK) status = p->digest(mask, r, c, e);
+  if (status == GG_OK) status = p->digest(mask, r, checksum ? c : nullptr, e);
   int32_t *d_lv = nullptr;
   uint32_t *d_pa = nullptr;
   float *d_di = nullptr;

@@ -189,12 +189,15 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def committed_traffic(kernel, workload):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+def committed_traffic(kernel, workload, scale):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if
+    one was captured on this workload at this scale."""
     p = os.path.join(REPO, "profiles", "traffic.json")
     try:
         d = json.load(open(p))
         e = d[workload][kernel]
+        if int(e["scale"]) != int(scale):
+            return None
         return float(e["bytes_per_launch"])
     except (OSError, KeyError, ValueError, TypeError):
         return None
@@ -422,7 +425,7 @@ def gpu_arm(args, dist):
     kname = {0: "push_lb", 1: "bfs_pull" if args.workload.startswith("bfs") else "pull_reduce"}[dom]
     peak, peak_kind = peaks()
     ach = per_mode[dom][1] / (per_mode[dom][0] / 1000.0) / 1e9 if per_mode[dom][0] > 0 else 0.0
-    traffic = committed_traffic(kname, args.workload)
+    traffic = committed_traffic(kname, args.workload, w["scale"])
     total_kernel_ms = per_mode[0][0] + per_mode[1][0]
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",

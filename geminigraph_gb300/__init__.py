@@ -89,6 +89,9 @@ def library():
         "gg_server_free": ([vp], i32),
         "gg_pool_bytes": ([vp, i32], u64),
         "gg_graph_set_bins": ([vp, u32, u32, u32], i32),
+        "gg_graph_set_sssp_delta": ([vp, ctypes.c_float], i32),
+        "gg_dump_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
+        "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_pr_layout": ([vp, i32], i32),
         "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
@@ -282,6 +285,9 @@ class Graph:
     def set_bins(self, light_deg, pull_chunk, pull_vector=1):
         _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk, 1 if pull_vector else 0))
 
+    def set_sssp_delta(self, delta):
+        _check(library().gg_graph_set_sssp_delta(self.h, float(delta)))
+
     def set_pr_layout(self, hot_sources):
         _check(library().gg_graph_set_pr_layout(self.h, 1 if hot_sources else 0))
 
@@ -405,6 +411,19 @@ def bc_batched(g, roots, outputs=True, timing=False):
         st.enable_call_timing()
     _check(library().gg_bc_batched(g.h, _ptr(r), len(r), _ptr(dep), _ptr(inv), _ptr(reached), ctypes.byref(st.s)))
     return dep, inv, reached, st
+
+
+def dump_vertex_array(array, path):
+    """core/graph.hpp:253 with one partition: the array's bytes in `path`."""
+    a = np.ascontiguousarray(array)
+    _check(library().gg_dump_vertex_array(_ptr(a), a.itemsize, len(a), os.fsencode(path)))
+
+
+def restore_vertex_array(path, vertices, dtype):
+    """core/graph.hpp:289: a vertex array back from `path` (its length must match)."""
+    a = np.empty(vertices, dtype)
+    _check(library().gg_restore_vertex_array(_ptr(a), a.itemsize, vertices, os.fsencode(path)))
+    return a
 
 
 def result_checksum(values, kind):

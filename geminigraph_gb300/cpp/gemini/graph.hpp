@@ -118,6 +118,15 @@ class Graph {
   void fill_vertex_array(T *array, T value) {
     for (VertexId v = 0; v < vertices; v++) array[v] = value;
   }
+  // core/graph.hpp:253-307: the array's bytes in a file (host or device array)
+  template <typename T>
+  void dump_vertex_array(T *array, std::string path) {
+    gemini::check(gg_dump_vertex_array(array, sizeof(T), vertices, path.c_str()), "dump_vertex_array");
+  }
+  template <typename T>
+  void restore_vertex_array(T *array, std::string path) {
+    gemini::check(gg_restore_vertex_array(array, sizeof(T), vertices, path.c_str()), "restore_vertex_array");
+  }
   // core/graph.hpp:327
   VertexSubset *alloc_vertex_subset() { return new VertexSubset(vertices); }
   // core/graph.hpp:311: one partition holds every vertex already.

@@ -15,10 +15,14 @@
 // over the union frontier's out-edges -- the reference's switch rule applied
 // to the union.  Lanes are independent, so a lane that finishes leaves its bit
 // clear and the others go on.
+#include <math.h>
+#include <string.h>
+
 #include <vector>
 
 #include "gg_engine.cuh"
 #include "gg_gen.h"
+
 #include "gg_lanes.cuh"
 
 namespace gg {
@@ -293,6 +297,97 @@ __device__ __forceinline__ u64 result_term(uint32_t v, uint32_t x) {
   return gg_mix64((u64)v * 0x9E3779B97F4A7C15ull + x);
 }
 
+// ---------------------------------------------------------------- bucketed SSSP
+static inline float host_float_of_bits(unsigned u) {
+  float f;
+  memcpy(&f, &u, sizeof f);
+  return f;
+}
+// A lane whose distance at v was lowered waits in pend[v] until that distance
+// is below the lane's threshold; then v expands for that lane (front[v]).
+// Relaxing in rising distance buckets re-relaxes far less than plain rounds,
+// and any relaxation order reaches the same fixpoint (every distance is the
+// least rounded path sum), so results stay bit-identical.
+__device__ __forceinline__ u64 shfl64(u64 x, int src) {
+  const unsigned lo = __shfl_sync(GG_FULL, (unsigned)x, src), hi = __shfl_sync(GG_FULL, (unsigned)(x >> 32), src);
+  return ((u64)hi << 32) | lo;
+}
+
+// Merges last step's lowered lanes (next) and admitted roots (front) into
+// pend, moves the lanes below threshold to front and queues their vertices;
+// per lane, the least distance still waiting (non-negative floats order like
+// their bits).  A warp takes 32 vertices and serves the ones with pending
+// lanes one at a time, thread t holding lanes t and t + 32.
+__global__ void __launch_bounds__(256)
+    msp_filter(uint32_t V, u64 *pend, u64 *next, u64 *front, const float *__restrict__ dist,
+               const float *__restrict__ thr, uint32_t *q, const uint32_t *__restrict__ out_deg, MsCounters *mc,
+               BucketCounters *bc) {
+  __shared__ unsigned s_min[LANES];
+  for (int i = threadIdx.x; i < LANES; i += blockDim.x) s_min[i] = 0xffffffffu;
+  __syncthreads();
+  const unsigned lane = lane_id();
+  const float t0 = thr[lane], t1 = thr[lane + 32];
+  unsigned mn0 = 0xffffffffu, mn1 = 0xffffffffu;
+  u64 t_alive = 0, t_expand = 0, t_edges = 0;
+  unsigned t_touched = 0;
+  const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
+  for (size_t g = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g * 32 < V; g += nwarps) {
+    const size_t v = g * 32 + lane;
+    u64 p = 0, nx = 0;
+    if (v < V) {
+      nx = next[v];
+      p = pend[v] | nx | front[v];
+    }
+    unsigned bal = __ballot_sync(GG_FULL, p != 0);
+    while (bal) {
+      const int j = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const size_t vj = g * 32 + j;
+      const u64 pj = shfl64(p, j);
+      const float *dv = dist + vj * LANES;
+      bool e0 = false, e1 = false;
+      if ((pj >> lane) & 1ull) {
+        const float x = dv[lane];
+        e0 = x < t0;
+        if (!e0 && __float_as_uint(x) < mn0) mn0 = __float_as_uint(x);
+      }
+      if ((pj >> (lane + 32)) & 1ull) {
+        const float x = dv[lane + 32];
+        e1 = x < t1;
+        if (!e1 && __float_as_uint(x) < mn1) mn1 = __float_as_uint(x);
+      }
+      const u64 E = (u64)__ballot_sync(GG_FULL, e0) | ((u64)__ballot_sync(GG_FULL, e1) << 32);
+      if ((int)lane == j) {
+        if (nx) next[vj] = 0;
+        front[vj] = E;
+        pend[vj] = pj & ~E;
+        if (E) {
+          q[atomicAdd(&mc->qlen, 1u)] = (uint32_t)vj;
+          t_edges += out_deg[vj];
+          t_touched += 1;
+        }
+      }
+      t_alive |= pj;
+      t_expand |= E;
+    }
+  }
+  atomicMin(&s_min[lane], mn0);
+  atomicMin(&s_min[lane + 32], mn1);
+  t_expand = warp_or64(t_expand);
+  if (lane == 0 && t_expand) atomicOr(&bc->expand, t_expand);
+  __syncthreads();
+  for (int i = threadIdx.x; i < LANES; i += blockDim.x)
+    if (s_min[i] != 0xffffffffu) atomicMin(&bc->minp[i], s_min[i]);
+  ms_flush(mc, t_alive, t_edges, t_touched);
+}
+
+__global__ void wmin_kernel(const float *__restrict__ w, size_t n, unsigned *out_bits_neg) {
+  bool neg = false;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    neg |= w[i] < 0.0f;
+  if (__any_sync(GG_FULL, neg) && lane_id() == 0) atomicOr(out_bits_neg, 1u);
+}
+
 // Per-lane digests of the lanes in mask: out[l] reached, out[64+l] checksum
 // (SUM only), out[128+l] out-degree sum of reached vertices.  BFS: x = hop
 // count; SSSP: x = the distance's float bits.  A warp walks vertices one at
@@ -495,7 +590,7 @@ size_t LanePool::bytes_needed(const gg_graph *g, Kind kind, bool parents) {
   b += (V + 2) * sizeof(u64) + scan_scratch_elems(V + 1) * sizeof(u64);       // degree prefix + scan
   b += (bitmap_words32(g->V) + V + 1) * sizeof(uint32_t) + scan_scratch_elems(V) * sizeof(uint32_t);
   if (kind == BFS) b += V * LANES * sizeof(uint32_t) * (parents ? 2 : 1);
-  else b += V * LANES * sizeof(float);
+  else b += V * LANES * sizeof(float) + V * sizeof(u64);
   return b + (1 << 20);
 }
 
@@ -519,8 +614,8 @@ int LanePool::open() {
   if (e == cudaSuccess) e = cudaMalloc(&roots_dev_, LANES * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&start_dev_, LANES * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&lanes_dev_, LANES * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&mc_, 256);
-  if (e == cudaSuccess) e = cudaMallocHost(&mc_host_, 256);
+  if (e == cudaSuccess) e = cudaMalloc(&mc_, 512);
+  if (e == cudaSuccess) e = cudaMallocHost(&mc_host_, 512);
   if (e == cudaSuccess) e = cudaMalloc(&out_dev_, 3 * LANES * sizeof(u64));
   if (e == cudaSuccess) e = cudaMallocHost(&out_host_, 3 * LANES * sizeof(u64));
   if (kind_ == BFS) {
@@ -533,6 +628,26 @@ int LanePool::open() {
     if (e == cudaSuccess) {
       fill_kernel<float><<<grid_for(V * LANES, 256, g_->num_sms, 16), 256, 0, s_>>>(dist_, V * LANES, 1e9f);
       e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&pend_, V * sizeof(u64));
+    if (e == cudaSuccess) e = cudaMemsetAsync(pend_, 0, V * sizeof(u64), s_);
+    if (e == cudaSuccess) e = cudaMalloc(&thr_dev_, LANES * sizeof(float));
+    if (e == cudaSuccess && !g_->wmin_known && g_->out.w && g_->nadj) {
+      unsigned *neg = nullptr;
+      e = cudaMalloc(&neg, sizeof(unsigned));
+      if (e == cudaSuccess) e = cudaMemsetAsync(neg, 0, sizeof(unsigned), s_);
+      if (e == cudaSuccess) {
+        wmin_kernel<<<grid_for(g_->nadj, 256, g_->num_sms, 8), 256, 0, s_>>>(g_->out.w, g_->nadj, neg);
+        e = cudaGetLastError();
+      }
+      unsigned h = 0;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&h, neg, sizeof(unsigned), cudaMemcpyDeviceToHost, s_);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+      if (neg) cudaFree(neg);
+      if (e == cudaSuccess) {
+        g_->wmin = h ? -1.0f : 0.0f;
+        g_->wmin_known = 1;
+      }
     }
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(front_, 0, V * sizeof(u64), s_);
@@ -552,7 +667,7 @@ int LanePool::open() {
 void LanePool::close() {
   if (s_) cudaStreamSynchronize(s_);
   void *bufs[] = {visit_, front_, next_, lvl_, par_, dist_, q_[0], q_[1], prefix_, scan64_, qpos_, scan32_,
-                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_};
+                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_, pend_, thr_dev_};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (mc_host_) cudaFreeHost(mc_host_);
@@ -561,6 +676,8 @@ void LanePool::close() {
   visit_ = front_ = next_ = nullptr;
   lvl_ = par_ = nullptr;
   dist_ = nullptr;
+  pend_ = nullptr;
+  thr_dev_ = nullptr;
   q_[0] = q_[1] = nullptr;
   prefix_ = scan64_ = nullptr;
   qpos_ = scan32_ = roots_dev_ = start_dev_ = nullptr;
@@ -588,6 +705,14 @@ int LanePool::admit(const uint32_t *roots, const int *lanes, int n) {
     }
     mask |= 1ull << lanes[i];
     start_[lanes[i]] = iter_;
+  }
+  if (kind_ == SSSP) {
+    // bucketing needs non-negative weights; the width is read per admission
+    if (used_ == 0) {
+      delta_ = g_->sssp_delta;
+      bucket_ = delta_ > 0.0f && g_->wmin_known && g_->wmin >= 0.0f;
+    }
+    for (int i = 0; i < n; i++) thr_[lanes[i]] = delta_;
   }
   const uint32_t V = g_->V;
   GG_CUDA(cudaMemcpyAsync(roots_dev_, roots, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s_));
@@ -719,10 +844,65 @@ int LanePool::sssp_step() {
   return GG_OK;
 }
 
+int LanePool::sssp_bucket_step() {
+  const uint32_t V = g_->V;
+  iter_ += 1;
+  BucketCounters *bc_dev = reinterpret_cast<BucketCounters *>(reinterpret_cast<char *>(mc_) + BUCKET_OFFSET);
+  const BucketCounters *bc_host =
+      reinterpret_cast<const BucketCounters *>(reinterpret_cast<const char *>(mc_host_) + BUCKET_OFFSET);
+  LaneCounters h;
+  u64 expand = 0;
+  // at most two rounds: a round that expands nothing raises every waiting
+  // lane's threshold past its least waiting distance
+  for (int round = 0; round < 2; round++) {
+    GG_CUDA(cudaMemcpyAsync(thr_dev_, thr_, sizeof(float) * LANES, cudaMemcpyHostToDevice, s_));
+    GG_CUDA(cudaMemsetAsync(mc_, 0, BUCKET_OFFSET + sizeof(u64), s_));
+    GG_CUDA(cudaMemsetAsync(bc_dev->minp, 0xff, sizeof(bc_dev->minp), s_));
+    msp_filter<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+        V, pend_, next_, front_, dist_, thr_dev_, q_[cur_], g_->out.deg, mc_, bc_dev);
+    launches += 1;
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(mc_host_, mc_, BUCKET_OFFSET + sizeof(BucketCounters), cudaMemcpyDeviceToHost, s_));
+    GG_CUDA(cudaStreamSynchronize(s_));
+    h = *mc_host_;
+    expand = bc_host->expand;
+    const u64 waiting = h.alive & ~expand;
+    for (int l = 0; l < LANES; l++) {
+      if (!((waiting >> l) & 1ull) || bc_host->minp[l] == 0xffffffffu) continue;
+      const float m = host_float_of_bits(bc_host->minp[l]);
+      float t = (floorf(m / delta_) + 1.0f) * delta_;
+      if (!(t > m)) t = nextafterf(m, 3.0e38f);
+      thr_[l] = t;
+    }
+    if (expand || !h.alive) break;
+  }
+  nq_ = h.qlen;
+  ae_ = h.edges;
+  if (tr_) tr_->add(0, ae_, h.touched);
+  active_ &= h.alive;
+  if (expand && nq_ && ae_) {
+    GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
+                                                               scan64_, s_, &launches)));
+    if (tr_) GG_TRY(tr_->kbegin());
+    msp_push<<<push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
+                                                              dist_, q_[cur_ ^ 1], mc_);
+    if (tr_) GG_TRY(tr_->kend());
+    launches += 1;
+  }
+  if (nq_) {
+    ms_clear_queue<<<grid_for(nq_, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
+    launches += 1;
+  }
+  GG_CUDA(cudaGetLastError());
+  qvalid_ = false;
+  return GG_OK;
+}
+
 int LanePool::step() {
   if (!active_) return GG_OK;
   calls_ += 1;
-  return kind_ == BFS ? bfs_step() : sssp_step();
+  if (kind_ == BFS) return bfs_step();
+  return bucket_ ? sssp_bucket_step() : sssp_step();
 }
 
 int LanePool::digest(u64 mask, u64 *reached, u64 *checksum, u64 *edges) {
@@ -880,4 +1060,13 @@ extern "C" uint64_t gg_result_checksum(const void *values, uint32_t vertices, in
     sum += gg_mix64((uint64_t)v * 0x9E3779B97F4A7C15ull + x);
   }
   return sum;
+}
+
+extern "C" int gg_graph_set_sssp_delta(gg_graph *g, float delta) {
+  if (!g || !(delta >= 0.0f)) {
+    gg::set_error("the bucket width must be >= 0");
+    return GG_ERR_INVALID;
+  }
+  g->sssp_delta = delta;
+  return GG_OK;
 }

@@ -148,6 +148,11 @@ struct gg_graph {
   uint32_t *pr_od = nullptr;          // V: out-degree in the new numbering
   bool pr_ready = false;
   int pr_layout = 1;                  // 0: PageRank pulls the plain incoming adjacency
+  // batched SSSP bucket width (0: plain Bellman-Ford rounds) and the least
+  // edge weight (bucketing needs none negative), found on first use
+  float sssp_delta = 0.0f;
+  int wmin_known = 0;
+  float wmin = 0.0f;
 };
 
 namespace gg {

@@ -19,6 +19,12 @@ struct LaneCounters {
   unsigned int touched;
   unsigned int qlen;
 };
+// Bucketed SSSP filter results, after the LaneCounters in the same buffer.
+struct BucketCounters {
+  unsigned long long expand;  // lanes with a vertex below its threshold
+  unsigned int minp[64];      // per lane, the least waiting distance (float bits)
+};
+constexpr size_t BUCKET_OFFSET = 64;
 
 class LanePool {
  public:
@@ -60,6 +66,7 @@ class LanePool {
   int build_queue();
   int bfs_step();
   int sssp_step();
+  int sssp_bucket_step();
   gg_graph *g_;
   Kind kind_;
   bool parents_;
@@ -69,6 +76,13 @@ class LanePool {
   unsigned long long *visit_ = nullptr, *front_ = nullptr, *next_ = nullptr;
   uint32_t *lvl_ = nullptr, *par_ = nullptr;
   float *dist_ = nullptr;
+  // bucketed SSSP (graph->sssp_delta > 0, no negative weights): lanes lowered
+  // but not yet expanded, and each lane's distance threshold
+  unsigned long long *pend_ = nullptr;
+  float *thr_dev_ = nullptr;
+  float thr_[64] = {};
+  float delta_ = 0.0f;
+  bool bucket_ = false;
   uint32_t *q_[2] = {nullptr, nullptr};
   unsigned long long *prefix_ = nullptr, *scan64_ = nullptr;
   uint32_t *qpos_ = nullptr, *scan32_ = nullptr;

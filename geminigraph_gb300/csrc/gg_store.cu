@@ -805,6 +805,80 @@ int gg_host_alloc(uint64_t bytes, void **out) {
   return GG_OK;
 }
 
+// core/graph.hpp:253-307 with one partition: the file is the array's bytes,
+// vertex 0 first.  `array` may be host or device memory.
+static bool is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int gg_dump_vertex_array(const void *array, uint64_t elem_size, uint32_t vertices, const char *path) {
+  if (!array || !path || elem_size == 0) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  const uint64_t bytes = elem_size * vertices;
+  std::vector<char> stage;
+  const char *src = (const char *)array;
+  if (is_device_ptr(array)) {
+    stage.resize(bytes);
+    GG_CUDA(cudaMemcpy(stage.data(), array, bytes, cudaMemcpyDeviceToHost));
+    src = stage.data();
+  }
+  FILE *f = fopen(path, "wb");
+  if (!f) {
+    set_error("cannot open %s for writing", path);
+    return GG_ERR_IO;
+  }
+  const size_t n = fwrite(src, 1, bytes, f);
+  const int rc = fclose(f);
+  if (n != bytes || rc != 0) {
+    set_error("short write to %s", path);
+    return GG_ERR_IO;
+  }
+  return GG_OK;
+}
+
+int gg_restore_vertex_array(void *array, uint64_t elem_size, uint32_t vertices, const char *path) {
+  if (!array || !path || elem_size == 0) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  const uint64_t bytes = elem_size * vertices;
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    set_error("cannot open %s", path);
+    return GG_ERR_IO;
+  }
+  fseek(f, 0, SEEK_END);
+  const long len = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  if (len < 0 || (uint64_t)len != bytes) {
+    fclose(f);
+    set_error("%s holds %ld bytes, the array %llu", path, len, (unsigned long long)bytes);
+    return GG_ERR_INVALID;
+  }
+  std::vector<char> stage;
+  const bool dev = is_device_ptr(array);
+  char *dst = (char *)array;
+  if (dev) {
+    stage.resize(bytes);
+    dst = stage.data();
+  }
+  const size_t n = fread(dst, 1, bytes, f);
+  fclose(f);
+  if (n != bytes) {
+    set_error("short read from %s", path);
+    return GG_ERR_IO;
+  }
+  if (dev) GG_CUDA(cudaMemcpy(array, stage.data(), bytes, cudaMemcpyHostToDevice));
+  return GG_OK;
+}
+
 int gg_host_free(void *p) {
   if (p) GG_CUDA(cudaFreeHost(p));
   return GG_OK;

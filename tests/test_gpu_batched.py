@@ -104,3 +104,19 @@ def test_bc_batched_rejects_bad_arguments(case):
         gg.bc_batched(g, [V])
     with pytest.raises((gg.GeminiError, ValueError)):
         gg.bc_batched(g, list(range(65)))
+
+
+@pytest.mark.parametrize("delta", [0.0, 0.03, 0.5])
+def test_sssp_batched_bucket_width_does_not_change_distances(case, delta):
+    """Plain rounds (0) and distance buckets of any width reach the same
+    distances, bit for bit, as the single-root SSSP."""
+    V, s, d, w, g = case
+    g.set_sssp_delta(delta)
+    roots = roots_for(V, s, 9, seed=50)
+    dist, reached, st = gg.sssp_batched(g, roots)
+    for i, r in enumerate(roots):
+        single, _ = g.sssp(r)
+        assert np.array_equal(dist[i].view(np.uint32), single.view(np.uint32)), f"lane {i} root {r}"
+    g.set_sssp_delta(0.0)
+    with pytest.raises(gg.GeminiError):
+        g.set_sssp_delta(-1.0)

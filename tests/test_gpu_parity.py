@@ -415,3 +415,20 @@ def test_autotune_objectives(tmp_path):
     assert np.array_equal(lv[0], bfs_levels(o.bfs(root)[0], root))
     with pytest.raises(gg.GeminiError):
         g.autotune(str(tmp_path), objective=())
+
+
+def test_dump_vertex_array_from_device(tmp_path):
+    """A device result array (the last call's, gg_result_device_ptr) dumps
+    to the same bytes as its host copy, and restores into device memory."""
+    import ctypes
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d, w)
+    dist, _ = g.sssp(root)
+    dev = gg.library().gg_result_device_ptr(g.h, 0)
+    assert dev
+    p = tmp_path / "dist.bin"
+    assert gg.library().gg_dump_vertex_array(ctypes.c_void_p(dev), 4, V, str(p).encode()) == 0
+    assert p.read_bytes() == dist.tobytes()
+    assert gg.library().gg_restore_vertex_array(ctypes.c_void_p(dev), 4, V, str(p).encode()) == 0
+    assert gg.library().gg_dump_vertex_array(ctypes.c_void_p(dev), 4, V, str(tmp_path / "again.bin").encode()) == 0
+    assert (tmp_path / "again.bin").read_bytes() == dist.tobytes()

@@ -74,3 +74,18 @@ def test_bad_arguments_return_status():
 def test_device_call_without_gpu_fails_loudly():
     with pytest.raises(gg.GeminiError):
         gg.Graph.generate(gg.RMAT, 8, 4, 1)
+
+
+def test_dump_and_restore_vertex_array(tmp_path):
+    """core/graph.hpp:253-307 with one partition: the file is the array's
+    bytes; a restore of a file of another length is an error, not an assert."""
+    a = np.arange(1000, dtype=np.float64) * 0.5
+    p = tmp_path / "ranks.bin"
+    gg.dump_vertex_array(a, str(p))
+    assert p.read_bytes() == a.tobytes()
+    b = gg.restore_vertex_array(str(p), 1000, np.float64)
+    assert np.array_equal(a, b)
+    with pytest.raises(gg.GeminiError):
+        gg.restore_vertex_array(str(p), 999, np.float64)
+    with pytest.raises(gg.GeminiError):
+        gg.restore_vertex_array(str(tmp_path / "missing.bin"), 10, np.uint32)

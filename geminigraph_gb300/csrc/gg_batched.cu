@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256)
           const uint32_t u = d.nbr[k];
           const u64 m = front[u] & need;
           if (m) {
-            ms_record((uint32_t)v, m, u, iter, lvl, par);
+            if (par) ms_record((uint32_t)v, m, u, iter, lvl, par);
             acc |= m;
             need &= ~m;
           }
@@ -154,8 +154,30 @@ __global__ void __launch_bounds__(256)
       }
       if (m) {
         const u64 won = m & ~atomicOr(next + v, m);
-        if (won) ms_record(v, won, u, iter, lvl, par);
+        if (won && par) ms_record(v, won, u, iter, lvl, par);
       }
+    }
+  }
+}
+
+// Levels of a dense step without parents: lvl[v][l] = iter for every lane
+// bit of next[v], one 256-byte row per vertex written by a warp (thread t:
+// lanes t and t + 32) instead of one scattered store per bit.
+__global__ void __launch_bounds__(256)
+    ms_mark_levels(uint32_t V, const u64 *__restrict__ next, uint32_t *lvl, uint32_t iter) {
+  const size_t nwarps = (size_t)gridDim.x * 8;
+  const unsigned lane = lane_id();
+  for (size_t g = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g * 32 < V; g += nwarps) {
+    const size_t v = g * 32 + lane;
+    const u64 m = v < V ? next[v] : 0ull;
+    unsigned bal = __ballot_sync(GG_FULL, m != 0);
+    while (bal) {
+      const int j = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const unsigned lo = __shfl_sync(GG_FULL, (unsigned)m, j), hi = __shfl_sync(GG_FULL, (unsigned)(m >> 32), j);
+      uint32_t *row = lvl + (g * 32 + j) * LANES;
+      if ((lo >> lane) & 1u) row[lane] = iter;
+      if ((hi >> lane) & 1u) row[lane + 32] = iter;
     }
   }
 }
@@ -795,6 +817,11 @@ int LanePool::bfs_step() {
           g_->in, active_, front_, visit_, next_, lvl_, par_, iter_);
       ms_big_finish<<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_);
       launches += 2;
+    }
+    if (!par_) {
+      ms_mark_levels<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(V, next_, lvl_,
+                                                                                              iter_);
+      launches += 1;
     }
     if (tr_) GG_TRY(tr_->kend());
     GG_TRY(read_counters(&h));

@@ -120,3 +120,17 @@ def test_sssp_batched_bucket_width_does_not_change_distances(case, delta):
     g.set_sssp_delta(0.0)
     with pytest.raises(gg.GeminiError):
         g.set_sssp_delta(-1.0)
+
+
+@pytest.mark.parametrize("n", [3, 64])
+def test_bfs_batched_levels_without_parents(case, n):
+    """Without parents the dense steps write levels in a separate pass; every
+    lane's levels still equal the single-root run's."""
+    V, s, d, w, g = case
+    roots = roots_for(V, s, max(n, 3), seed=200 + n)[:n]
+    lv, pa, reached, edges, st = gg.bfs_batched(g, roots, levels=True, parents=False)
+    assert pa is None
+    for i, r in enumerate(roots):
+        parent, single = g.bfs(r)
+        assert np.array_equal(lv[i], bfs_levels(parent, r)), f"lane {i} root {r}"
+        assert int(edges[i]) == single.active_edges_total

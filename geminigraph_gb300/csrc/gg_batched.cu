@@ -160,26 +160,53 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Levels of a dense step without parents: lvl[v][l] = iter for every lane
-// bit of next[v], one 256-byte row per vertex written by a warp (thread t:
-// lanes t and t + 32) instead of one scattered store per bit.
+// Levels of a step without parents: lvl[v][l] = iter for every lane bit of
+// next[v], one 256-byte row per vertex written by a warp (thread t: lanes t
+// and t + 32) instead of one scattered store per bit; the same pass adds the
+// newly reached vertices and their out-degrees to the per-lane sums.
 __global__ void __launch_bounds__(256)
-    ms_mark_levels(uint32_t V, const u64 *__restrict__ next, uint32_t *lvl, uint32_t iter) {
+    ms_mark_levels(uint32_t V, const u64 *__restrict__ next, uint32_t *lvl, uint32_t iter,
+                   const uint32_t *__restrict__ out_deg, u64 *lane_sum) {
+  __shared__ u64 s_sum[2 * LANES];
+  for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x) s_sum[i] = 0;
+  __syncthreads();
   const size_t nwarps = (size_t)gridDim.x * 8;
   const unsigned lane = lane_id();
+  u64 c0 = 0, c1 = 0, e0 = 0, e1 = 0;
   for (size_t g = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g * 32 < V; g += nwarps) {
     const size_t v = g * 32 + lane;
     const u64 m = v < V ? next[v] : 0ull;
+    const uint32_t dg = m ? out_deg[v] : 0u;
     unsigned bal = __ballot_sync(GG_FULL, m != 0);
     while (bal) {
       const int j = __ffs(bal) - 1;
       bal &= bal - 1;
       const unsigned lo = __shfl_sync(GG_FULL, (unsigned)m, j), hi = __shfl_sync(GG_FULL, (unsigned)(m >> 32), j);
+      const uint32_t dj = __shfl_sync(GG_FULL, dg, j);
       uint32_t *row = lvl + (g * 32 + j) * LANES;
-      if ((lo >> lane) & 1u) row[lane] = iter;
-      if ((hi >> lane) & 1u) row[lane + 32] = iter;
+      if ((lo >> lane) & 1u) {
+        row[lane] = iter;
+        c0 += 1;
+        e0 += dj;
+      }
+      if ((hi >> lane) & 1u) {
+        row[lane + 32] = iter;
+        c1 += 1;
+        e1 += dj;
+      }
     }
   }
+  if (c0) {
+    atomicAdd(&s_sum[lane], c0);
+    atomicAdd(&s_sum[LANES + lane], e0);
+  }
+  if (c1) {
+    atomicAdd(&s_sum[lane + 32], c1);
+    atomicAdd(&s_sum[LANES + lane + 32], e1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x)
+    if (s_sum[i]) atomicAdd(lane_sum + i, s_sum[i]);
 }
 
 // visit |= next for the long-list vertices, and their tallies.
@@ -236,7 +263,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
         if (m && (m & ~*(volatile u64 *)(next + v))) {
           const u64 old = atomicOr(next + v, m);
           const u64 won = m & ~old;
-          if (won) ms_record(v, won, u, iter, lvl, par);
+          if (won && par) ms_record(v, won, u, iter, lvl, par);
           fresh = old == 0;
         }
       }
@@ -298,7 +325,8 @@ __global__ void lanes_reset_dist(float *dist, uint32_t V, u64 mask) {
 
 // Roots into lanes: frontier bit, visited bit / distance 0, discovery iteration.
 __global__ void lanes_admit(const uint32_t *roots, const int *lanes, int n, u64 *front, u64 *visit, uint32_t *lvl,
-                            uint32_t *par, float *dist, uint32_t iter, const uint32_t *out_deg, MsCounters *mc) {
+                            uint32_t *par, float *dist, uint32_t iter, const uint32_t *out_deg, MsCounters *mc,
+                            u64 *lane_sum) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   u64 edges = 0;
   for (int i = 0; i < n; i++) {
@@ -310,6 +338,10 @@ __global__ void lanes_admit(const uint32_t *roots, const int *lanes, int n, u64 
     if (lvl) lvl[(size_t)r * LANES + l] = iter;
     if (par) par[(size_t)r * LANES + l] = r;
     if (dist) dist[(size_t)r * LANES + l] = 0.0f;
+    if (lane_sum) {
+      lane_sum[l] = 1;
+      lane_sum[LANES + l] = out_deg[r];
+    }
   }
   mc->edges = edges;
 }
@@ -641,6 +673,7 @@ int LanePool::open() {
   if (e == cudaSuccess) e = cudaMalloc(&out_dev_, 3 * LANES * sizeof(u64));
   if (e == cudaSuccess) e = cudaMallocHost(&out_host_, 3 * LANES * sizeof(u64));
   if (kind_ == BFS) {
+    if (e == cudaSuccess && !parents_) e = cudaMalloc(&lane_sum_, 2 * LANES * sizeof(u64));
     if (e == cudaSuccess) e = cudaMalloc(&visit_, V * sizeof(u64));
     if (e == cudaSuccess) e = cudaMalloc(&lvl_, V * LANES * sizeof(uint32_t));
     if (e == cudaSuccess && parents_) e = cudaMalloc(&par_, V * LANES * sizeof(uint32_t));
@@ -689,7 +722,7 @@ int LanePool::open() {
 void LanePool::close() {
   if (s_) cudaStreamSynchronize(s_);
   void *bufs[] = {visit_, front_, next_, lvl_, par_, dist_, q_[0], q_[1], prefix_, scan64_, qpos_, scan32_,
-                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_, pend_, thr_dev_};
+                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_, pend_, thr_dev_, lane_sum_};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (mc_host_) cudaFreeHost(mc_host_);
@@ -700,6 +733,7 @@ void LanePool::close() {
   dist_ = nullptr;
   pend_ = nullptr;
   thr_dev_ = nullptr;
+  lane_sum_ = nullptr;
   q_[0] = q_[1] = nullptr;
   prefix_ = scan64_ = nullptr;
   qpos_ = scan32_ = roots_dev_ = start_dev_ = nullptr;
@@ -745,7 +779,8 @@ int LanePool::admit(const uint32_t *roots, const int *lanes, int n) {
   else
     lanes_reset_dist<<<grid_for((size_t)V * LANES, 256, g_->num_sms, 16), 256, 0, s_>>>(dist_, V, mask);
   GG_CUDA(cudaMemsetAsync(mc_, 0, sizeof(LaneCounters), s_));
-  lanes_admit<<<1, 32, 0, s_>>>(roots_dev_, lanes_dev_, n, front_, visit_, lvl_, par_, dist_, iter_, g_->out.deg, mc_);
+  lanes_admit<<<1, 32, 0, s_>>>(roots_dev_, lanes_dev_, n, front_, visit_, lvl_, par_, dist_, iter_, g_->out.deg, mc_,
+                                lane_sum_);
   launches += 2;
   GG_CUDA(cudaGetLastError());
   LaneCounters h;
@@ -802,6 +837,11 @@ int LanePool::bfs_step() {
                                                                         g_->out.deg, mc_);
     ms_clear_queue<<<grid_for(nq_ ? nq_ : 1, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
     launches += 2;
+    if (!par_ && hq.qlen) {
+      ms_mark_levels<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+          V, next_, lvl_, iter_, g_->out.deg, lane_sum_);
+      launches += 1;
+    }
     GG_TRY(read_counters(&h));
     nq_ = h.qlen;
     qvalid_ = true;
@@ -819,8 +859,8 @@ int LanePool::bfs_step() {
       launches += 2;
     }
     if (!par_) {
-      ms_mark_levels<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(V, next_, lvl_,
-                                                                                              iter_);
+      ms_mark_levels<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+          V, next_, lvl_, iter_, g_->out.deg, lane_sum_);
       launches += 1;
     }
     if (tr_) GG_TRY(tr_->kend());
@@ -936,6 +976,17 @@ int LanePool::digest(u64 mask, u64 *reached, u64 *checksum, u64 *edges) {
   mask &= used_;
   if (!mask) return GG_OK;
   const uint32_t V = g_->V;
+  if (kind_ == BFS && lane_sum_ && !checksum) {
+    // the level passes kept the sums: no scan of the graph
+    GG_CUDA(cudaMemcpyAsync(out_host_, lane_sum_, 2 * LANES * sizeof(u64), cudaMemcpyDeviceToHost, s_));
+    GG_CUDA(cudaStreamSynchronize(s_));
+    for (int l = 0; l < LANES; l++) {
+      if (!((mask >> l) & 1ull)) continue;
+      if (reached) reached[l] = out_host_[l];
+      if (edges) edges[l] = out_host_[LANES + l];
+    }
+    return GG_OK;
+  }
   GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
   GG_CUDA(cudaMemsetAsync(out_dev_, 0, 3 * LANES * sizeof(u64), s_));
   const unsigned grid = grid_for((size_t)V * 32, 256, g_->num_sms, 8);

@@ -90,6 +90,9 @@ class LanePool {
   int *lanes_dev_ = nullptr;
   LaneCounters *mc_ = nullptr, *mc_host_ = nullptr;
   unsigned long long *out_dev_ = nullptr, *out_host_ = nullptr;  // 3 x 64 digest values
+  // BFS without parents: per lane, vertices reached and their out-degree sum,
+  // kept up to date by the level pass of every step (2 x 64)
+  unsigned long long *lane_sum_ = nullptr;
   // host state
   unsigned long long used_ = 0, active_ = 0;
   unsigned long long ae_ = 0;

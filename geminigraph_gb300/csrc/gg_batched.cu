@@ -106,13 +106,23 @@ __global__ void __launch_bounds__(256)
       u64 need = ~vis & alive;
       const unsigned long long b = d.off[v], e = d.off[v + 1];
       if (need && e - b <= d.light) {
-        for (unsigned long long k = b; k < e && need; k++) {
-          const uint32_t u = d.nbr[k];
-          const u64 m = front[u] & need;
-          if (m) {
-            if (par) ms_record((uint32_t)v, m, u, iter, lvl, par);
-            acc |= m;
-            need &= ~m;
+        // four independent neighbour / frontier loads per step; within a
+        // step any in-neighbour on a lane's frontier is a valid parent
+        for (unsigned long long k = b; k < e && need; k += 4) {
+          uint32_t u[4];
+          u64 f[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) u[i] = k + i < e ? d.nbr[k + i] : 0u;
+#pragma unroll
+          for (int i = 0; i < 4; i++) f[i] = k + i < e ? front[u[i]] : 0ull;
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const u64 m = f[i] & need;
+            if (m) {
+              if (par) ms_record((uint32_t)v, m, u[i], iter, lvl, par);
+              acc |= m;
+              need &= ~m;
+            }
           }
         }
       }

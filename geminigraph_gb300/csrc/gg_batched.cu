@@ -170,6 +170,47 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The same for a sparse step, over its queue of newly reached vertices: a
+// warp per vertex (thread t: lanes t and t + 32).
+__global__ void __launch_bounds__(256)
+    ms_mark_levels_q(const uint32_t *__restrict__ q, const unsigned *n_dev, const u64 *__restrict__ next,
+                     uint32_t *lvl, uint32_t iter, const uint32_t *__restrict__ out_deg, u64 *lane_sum) {
+  __shared__ u64 s_sum[2 * LANES];
+  for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x) s_sum[i] = 0;
+  __syncthreads();
+  const uint32_t n = *n_dev;
+  const size_t nwarps = (size_t)gridDim.x * 8;
+  const unsigned lane = lane_id();
+  u64 c0 = 0, c1 = 0, e0 = 0, e1 = 0;
+  for (size_t i = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
+    const uint32_t v = q[i];
+    const u64 m = next[v];
+    const uint32_t dg = out_deg[v];
+    uint32_t *row = lvl + (size_t)v * LANES;
+    if ((m >> lane) & 1ull) {
+      row[lane] = iter;
+      c0 += 1;
+      e0 += dg;
+    }
+    if ((m >> (lane + 32)) & 1ull) {
+      row[lane + 32] = iter;
+      c1 += 1;
+      e1 += dg;
+    }
+  }
+  if (c0) {
+    atomicAdd(&s_sum[lane], c0);
+    atomicAdd(&s_sum[LANES + lane], e0);
+  }
+  if (c1) {
+    atomicAdd(&s_sum[lane + 32], c1);
+    atomicAdd(&s_sum[LANES + lane + 32], e1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x)
+    if (s_sum[i]) atomicAdd(lane_sum + i, s_sum[i]);
+}
+
 // Levels of a step without parents: lvl[v][l] = iter for every lane bit of
 // next[v], one 256-byte row per vertex written by a warp (thread t: lanes t
 // and t + 32) instead of one scattered store per bit; the same pass adds the
@@ -283,8 +324,11 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 }
 
 // After a push: visit |= next over the touched queue, and the tallies.
-__global__ void ms_push_finish(const uint32_t *__restrict__ q, uint32_t n, u64 *visit, const u64 *__restrict__ next,
-                               const uint32_t *__restrict__ out_deg, MsCounters *mc) {
+// n_dev: the queue length the push kernel counted (read on the device, so
+// the host does not wait between the two kernels).
+__global__ void ms_push_finish(const uint32_t *__restrict__ q, const unsigned *n_dev, u64 *visit,
+                               const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg, MsCounters *mc) {
+  const uint32_t n = *n_dev;
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ((size_t)n + 255) / 256 * 256;
@@ -840,16 +884,14 @@ int LanePool::bfs_step() {
       if (tr_) GG_TRY(tr_->kend());
       launches += 1;
     }
-    LaneCounters hq;
-    GG_TRY(read_counters(&hq));
-    if (hq.qlen)
-      ms_push_finish<<<grid_for(hq.qlen, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_ ^ 1], hq.qlen, visit_, next_,
-                                                                        g_->out.deg, mc_);
+    // the queue length stays on the device: one host wait per step
+    const unsigned *qlen_dev = &mc_->qlen;
+    ms_push_finish<<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, visit_, next_, g_->out.deg, mc_);
     ms_clear_queue<<<grid_for(nq_ ? nq_ : 1, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
     launches += 2;
-    if (!par_ && hq.qlen) {
-      ms_mark_levels<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-          V, next_, lvl_, iter_, g_->out.deg, lane_sum_);
+    if (!par_) {
+      ms_mark_levels_q<<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, next_, lvl_, iter_, g_->out.deg,
+                                                       lane_sum_);
       launches += 1;
     }
     GG_TRY(read_counters(&h));

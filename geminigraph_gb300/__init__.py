@@ -89,6 +89,7 @@ def library():
         "gg_server_free": ([vp], i32),
         "gg_pool_bytes": ([vp, i32], u64),
         "gg_graph_set_bins": ([vp, u32, u32, u32], i32),
+        "gg_bfs_many": ([vp, vp, i32, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_sssp_delta": ([vp, ctypes.c_float], i32),
         "gg_dump_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
@@ -287,6 +288,16 @@ class Graph:
 
     def set_sssp_delta(self, delta):
         _check(library().gg_graph_set_sssp_delta(self.h, float(delta)))
+
+    def bfs_many(self, roots, outputs):
+        """Single-root BFS of each root in turn, result i copied into
+        outputs[i] (a host array of V uint32, or None) while run i + 1
+        computes; returns the summed RunStats."""
+        r = np.ascontiguousarray(roots, np.uint32)
+        ptrs = (ctypes.c_void_p * max(len(r), 1))(*[(o.ctypes.data if o is not None else None) for o in outputs])
+        st = RunStats()
+        _check(library().gg_bfs_many(self.h, _ptr(r), len(r), ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(st.s)))
+        return st
 
     def set_pr_layout(self, hot_sources):
         _check(library().gg_graph_set_pr_layout(self.h, 1 if hot_sources else 0))

@@ -1,5 +1,7 @@
 // BFS (toolkits/bfs.cpp) and PageRank (toolkits/pagerank.cpp) on the
 // device engine, plus the process_vertices reduction of the switch.
+#include <string.h>
+
 #include "gg_engine.cuh"
 
 namespace gg {
@@ -27,7 +29,9 @@ __global__ void bfs_root(uint32_t *parent, uint32_t root, uint32_t *visited, uin
   ctr->qlen = 1;
 }
 
-static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_stats *st) {
+// parent_slot: the workspace array the parent tree is written to (the
+// pipelined calls alternate between two).
+static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_stats *st, WsSlot parent_slot = WS_S0) {
   if (root >= g->V) {
     set_error("root %u >= vertices %u", root, g->V);
     return GG_ERR_INVALID;
@@ -36,7 +40,7 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
   const uint32_t V = g->V;
   const size_t words = bitmap_words32(V);
   uint32_t *parent, *visited, *bm[2], *q[2];
-  GG_TRY(ws(g, WS_S0, V, &parent));
+  GG_TRY(ws(g, parent_slot, V, &parent));
   GG_TRY(ws(g, WS_BM0, words, &visited));
   GG_TRY(ws(g, WS_BM1, words, &bm[0]));
   GG_TRY(ws(g, WS_BM2, words, &bm[1]));
@@ -292,6 +296,73 @@ int gg_graph_set_pr_layout(gg_graph *g, int hot_sources) {
   g->pr_layout = hot_sources ? 1 : 0;
   if (!g->pr_layout) pr_layout_free(g);
   return GG_OK;
+}
+
+int gg_bfs_many(gg_graph *g, const uint32_t *roots, int n, uint32_t *const *parents, gg_run_stats *stats) {
+  if (!g || !roots || n < 0 || (n && !parents)) {
+    set_error("null argument");
+    return GG_ERR_INVALID;
+  }
+  for (int i = 0; i < n; i++)
+    if (roots[i] >= g->V) {
+      set_error("root %u >= vertices %u", roots[i], g->V);
+      return GG_ERR_INVALID;
+    }
+  GG_CUDA(cudaSetDevice(g->device));
+  if (stats) {
+    stats->calls = 0;
+    stats->active_edges_total = 0;
+    stats->device_ms = 0;
+    stats->kernel_launches = 0;
+  }
+  const WsSlot slot[2] = {WS_S0, WS_PIPE};
+  cudaStream_t cs = nullptr;
+  cudaEvent_t done[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+  int status = GG_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+    e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) status = cuda_status(e, "pipeline set-up");
+  for (int i = 0; i < n && status == GG_OK; i++) {
+    const int b = i & 1;
+    // the buffer's previous result must be on the host before it is reused
+    if (i >= 2) e = cudaStreamWaitEvent(g->stream, copied[b], 0);
+    if (e != cudaSuccess) {
+      status = cuda_status(e, "pipeline wait");
+      break;
+    }
+    gg_run_stats one;
+    memset(&one, 0, sizeof(one));
+    status = bfs_run(g, roots[i], nullptr, &one, slot[b]);
+    if (status != GG_OK) break;
+    if (stats) {
+      stats->calls += one.calls;
+      stats->active_edges_total += one.active_edges_total;
+      stats->device_ms += one.device_ms;
+      stats->kernel_launches += one.kernel_launches;
+    }
+    uint32_t *dev = nullptr;
+    status = ws(g, slot[b], g->V, &dev);
+    if (status != GG_OK) break;
+    e = cudaEventRecord(done[b], g->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, done[b], 0);
+    if (e == cudaSuccess && parents[i])
+      e = cudaMemcpyAsync(parents[i], dev, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaEventRecord(copied[b], cs);
+    if (e != cudaSuccess) status = cuda_status(e, "pipeline copy");
+  }
+  if (cs) {
+    const cudaError_t e2 = cudaStreamSynchronize(cs);
+    if (status == GG_OK && e2 != cudaSuccess) status = cuda_status(e2, "pipeline copy");
+    cudaStreamDestroy(cs);
+  }
+  for (int b = 0; b < 2; b++) {
+    if (done[b]) cudaEventDestroy(done[b]);
+    if (copied[b]) cudaEventDestroy(copied[b]);
+  }
+  return status;
 }
 
 int gg_pagerank(gg_graph *g, int iterations, double *ranks, double *deltas, gg_run_stats *stats) {

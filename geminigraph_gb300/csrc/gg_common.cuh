@@ -98,6 +98,7 @@ enum WsSlot {
   WS_SCAN,                              // scan scratch
   WS_HUBSUM,                            // per-iteration counters (PageRank)
   WS_PARTIAL,                           // per-chunk partial results of heavy lists
+  WS_PIPE,                              // second result buffer of the pipelined calls
   WS_QPOS,                              // per-word queue positions (queue_from_bitmap)
   WS_STAMP,                             // per-vertex activation stamps (small sparse runs)
   WS_SMALL,                             // SmallRun state and its trace rows
@@ -114,7 +115,9 @@ struct Workspace {
   size_t bytes[WS_NSLOTS] = {};
   Counters *ctr = nullptr;       // device
   Counters *ctr_host = nullptr;  // pinned mirror
+  void *stage = nullptr;         // page-locked, device-mapped staging for read_small
 };
+constexpr size_t STAGE_BYTES_HOST = 64 * 1024;
 
 class LanePool;
 void pools_destroy(gg_graph *g);
@@ -166,6 +169,11 @@ inline int ws(gg_graph *g, WsSlot slot, size_t count, T **out) {
 int ws_free_all(gg_graph *g);
 int counters_reset(gg_graph *g);
 int counters_read(gg_graph *g, Counters *out);
+// Small device-to-host reads on the graph's stream, copied by the SMs into
+// page-locked device-mapped memory: they do not wait behind a large
+// copy-engine transfer running on another stream (pipelined result copies).
+// Waits for the stream.
+int read_small(gg_graph *g, void *dst, const void *src, size_t bytes);
 
 inline size_t bitmap_words32(uint32_t V) { return 2 * ((size_t)V / 64 + 1); }
 inline unsigned grid_for(size_t work, int threads, int num_sms, int per_sm = 8) {

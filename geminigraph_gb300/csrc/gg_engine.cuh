@@ -776,10 +776,7 @@ struct Launch {
     queue_scatter<<<grid_for(words, 256, g->num_sms, 8), 256, 0, g->stream>>>(bm, mask, words, pos, q);
     launches += 1;
     GG_CUDA(cudaGetLastError());
-    GG_CUDA(cudaMemcpyAsync(g->ws.ctr_host, pos + words, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
-    GG_CUDA(cudaStreamSynchronize(g->stream));
-    *n = *(uint32_t *)g->ws.ctr_host;
-    return GG_OK;
+    return read_small(g, n, pos + words, sizeof(uint32_t));
   }
   // Runs consecutive small sparse calls on the device (see SmallRun).  On
   // entry q[*cur] holds the active vertices with out-degree > 0 (nq of them)
@@ -853,15 +850,10 @@ struct Launch {
         break;
       }
       launches += batch * (snap_msg ? 2 : 1);
-      e = cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h_ae.data(), tr_ae, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(h_act.data(), tr_act, sizeof(unsigned) * batch, cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) {
-        status = cuda_status(e, "small run");
-        break;
-      }
+      status = read_small(g, &h, st, sizeof(h));
+      if (status == GG_OK) status = read_small(g, h_ae.data(), tr_ae, sizeof(unsigned long long) * batch);
+      if (status == GG_OK) status = read_small(g, h_act.data(), tr_act, sizeof(unsigned) * batch);
+      if (status != GG_OK) break;
       for (uint32_t r = 0; r < h.calls; r++) {
         tr.add(0, h_ae[r], h_act[r]);
         *n_act = h_act[r];

@@ -68,8 +68,28 @@ int ws_free_all(gg_graph *g) {
   }
   if (w.ctr) cudaFree(w.ctr);
   if (w.ctr_host) cudaFreeHost(w.ctr_host);
+  if (w.stage) cudaFreeHost(w.stage);
   w.ctr = nullptr;
   w.ctr_host = nullptr;
+  w.stage = nullptr;
+  return GG_OK;
+}
+
+__global__ void copy_words_to_mapped(const uint32_t *__restrict__ src, uint32_t *dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+int read_small(gg_graph *g, void *dst, const void *src, size_t bytes) {
+  if (!g->ws.stage || bytes > STAGE_BYTES_HOST || (bytes & 3) || ((uintptr_t)src & 3)) {
+    GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g->stream));
+    GG_CUDA(cudaStreamSynchronize(g->stream));
+    return GG_OK;
+  }
+  copy_words_to_mapped<<<1, 256, 0, g->stream>>>((const uint32_t *)src, (uint32_t *)g->ws.stage, bytes / 4);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  memcpy(dst, g->ws.stage, bytes);
   return GG_OK;
 }
 
@@ -78,12 +98,7 @@ int counters_reset(gg_graph *g) {
   return GG_OK;
 }
 
-int counters_read(gg_graph *g, Counters *out) {
-  GG_CUDA(cudaMemcpyAsync(g->ws.ctr_host, g->ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, g->stream));
-  GG_CUDA(cudaStreamSynchronize(g->stream));
-  *out = *g->ws.ctr_host;
-  return GG_OK;
-}
+int counters_read(gg_graph *g, Counters *out) { return read_small(g, out, g->ws.ctr, sizeof(Counters)); }
 
 int Trace::kbegin() {
   if (!timing()) return GG_OK;
@@ -720,6 +735,7 @@ static int graph_create(int device, uint32_t V, int weighted, int symmetric, gg_
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaMalloc(&g->ws.ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMallocHost(&g->ws.ctr_host, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaHostAlloc(&g->ws.stage, STAGE_BYTES_HOST, cudaHostAllocMapped);
   if (e != cudaSuccess) {
     graph_destroy(g);
     return cuda_status(e, "graph create");

@@ -150,6 +150,16 @@ int gg_bfs(gg_graph *g, uint32_t root, uint32_t *parent, gg_run_stats *stats);
 
 /* toolkits/pagerank.cpp:26-129: double ranks after `iterations` iterations;
  * deltas (may be NULL) receives the `iterations` values printed as delta(i). */
+/* n single-root BFS runs (each exactly gg_bfs) back to back, the parent tree
+ * of run i copied to parents[i] (host memory, V entries; NULL skips it) on a
+ * second stream while run i + 1 computes, from two alternating device
+ * buffers.  With page-locked host memory (gg_host_alloc) the copies hide
+ * behind the next run: the runs' own small readbacks go through the SMs
+ * into mapped memory, so they never queue behind a result copy.
+ * stats: calls, active_edges_total, device_ms and kernel_launches summed over
+ * the runs (no per-call rows).  No reference counterpart: the reference's
+ * bfs main() runs compute() six times in a row (toolkits/bfs.cpp:111-139). */
+int gg_bfs_many(gg_graph *g, const uint32_t *roots, int n, uint32_t *const *parents, gg_run_stats *stats);
 int gg_pagerank(gg_graph *g, int iterations, double *ranks, double *deltas, gg_run_stats *stats);
 
 /* As gg_pagerank in float arithmetic (float ranks, float sums). */

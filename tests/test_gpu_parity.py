@@ -432,3 +432,24 @@ def test_dump_vertex_array_from_device(tmp_path):
     assert gg.library().gg_restore_vertex_array(ctypes.c_void_p(dev), 4, V, str(p).encode()) == 0
     assert gg.library().gg_dump_vertex_array(ctypes.c_void_p(dev), 4, V, str(tmp_path / "again.bin").encode()) == 0
     assert (tmp_path / "again.bin").read_bytes() == dist.tobytes()
+
+
+def test_bfs_many_equals_single_runs():
+    """gg_bfs_many: each run's parent tree lands in its host array and equals
+    gg_bfs on the same root; a NULL output skips the copy."""
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d)
+    deg = np.bincount(s, minlength=V)
+    roots = gg.pick_roots(deg, 5, 31)
+    outs = [np.empty(V, np.uint32) for _ in roots]
+    outs[3] = None
+    st = g.bfs_many(roots, outs)
+    total = 0
+    for r, o in zip(roots, outs):
+        parent, single = g.bfs(r)
+        total += single.active_edges_total
+        if o is not None:
+            assert np.array_equal(bfs_levels(o, r), bfs_levels(parent, r))
+    assert st.active_edges_total == total
+    with pytest.raises(gg.GeminiError):
+        g.bfs_many([V], [None])

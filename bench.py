@@ -11,8 +11,10 @@ engine) / time.
 
   value      graph and root resident in HBM; device time of each BFS
              (CUDA events on the library's stream), results left on device
-  e2e        the same BFS through the C ABI with the parent array copied back
-             to pinned host memory inside the timed region (wall clock)
+  e2e        the same roots through the C ABI with every parent array copied
+             back to pinned host memory inside the timed region (wall clock):
+             gg_bfs_many (each copy overlaps the next root's BFS); the
+             one-gg_bfs-call-per-root figure is e2e.sync_value
   roofline   the dominant edge kernel's algorithmic bytes / its event time
   cpu_baseline  the reference's own BFS (oracle/_ref, built from the
              reference sources) on this host's cores on a bounded R-MAT

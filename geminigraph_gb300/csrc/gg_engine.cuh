@@ -22,6 +22,8 @@
 
 #include <string.h>
 
+#include <cooperative_groups.h>
+
 #include "gg_common.cuh"
 #include "gg_scan.cuh"
 
@@ -492,6 +494,7 @@ constexpr uint32_t SMALL_BATCH = 512;        // calls enqueued per host round tr
 constexpr uint32_t SMALL_MAX_QUEUE = 65536;  // largest queue a small call takes
 constexpr unsigned long long SMALL_MAX_AE = 1ull << 20;
 constexpr uint32_t SMALL_MAX_DEG = 1024;     // largest out-degree in a small call's queue
+constexpr int COOP_BLOCKS = 32;              // blocks of a cooperative small run (all resident)
 
 struct SmallRun {
   unsigned long long ae;         // active_edges of the call about to run
@@ -506,6 +509,18 @@ struct SmallRun {
   unsigned int maxdeg;           // largest out-degree in the queue of the call about to run
   Counters next;                 // accumulators of the current call
 };
+
+// Queue append from divergent lanes: one atomic per group of lanes that
+// reach this point together.
+__device__ __forceinline__ void queue_append_any(uint32_t v, uint32_t *q, unsigned *qlen) {
+  const unsigned am = __activemask();
+  const int leader = __ffs(am) - 1;
+  const unsigned lane = lane_id();
+  unsigned base = 0;
+  if ((int)lane == leader) base = atomicAdd(qlen, (unsigned)__popc(am));
+  base = __shfl_sync(am, base, leader);
+  q[base + __popc(am & ((1u << lane) - 1u))] = v;
+}
 
 // Activation inside a small push call: stamp-deduplicated unless the op's
 // slot already lets one thread win (BFS's CAS).  Lanes may be divergent.
@@ -522,24 +537,17 @@ __device__ __forceinline__ void small_activate(uint32_t v, SmallRun *st, uint32_
   t.edges += od;
   t.maxdeg = od > t.maxdeg ? od : t.maxdeg;
   if (in_deg) t.in_edges += in_deg[v];
-  if (od > 0) q_out[atomicAdd(&st->next.qlen, 1u)] = v;
+  if (od > 0) queue_append_any(v, q_out, &st->next.qlen);
 }
 
+// One small push call over q_in (n entries): slots, activation, and the
+// call's tally flushed into st->next.  Every thread of the block calls it.
 template <class Op, bool kUnique>
-__global__ void __launch_bounds__(SMALL_THREADS)
-    push_small(SmallRun *st, const uint32_t *__restrict__ q_in, uint32_t *__restrict__ q_out, Dir d, Op op,
-               uint32_t *stamp, uint32_t *visited, const uint32_t *__restrict__ out_deg,
-               const uint32_t *__restrict__ in_deg, unsigned long long *tr_ae, unsigned int *tr_act) {
-  __shared__ unsigned s_go, s_n, s_level, s_last;
-  if (threadIdx.x == 0) {
-    s_go = st->go;
-    s_n = st->n;
-    s_level = st->level;
-  }
-  __syncthreads();
-  if (!s_go) return;
-  const uint32_t n = s_n;
-  const unsigned level = s_level, lane = lane_id();
+__device__ __forceinline__ void small_call(SmallRun *st, const uint32_t *__restrict__ q_in, uint32_t *__restrict__ q_out,
+                                           const Dir &d, const Op &op, uint32_t *stamp, uint32_t *visited,
+                                           const uint32_t *__restrict__ out_deg, const uint32_t *__restrict__ in_deg,
+                                           uint32_t n, unsigned level) {
+  const unsigned lane = lane_id();
   Tally t;
   const size_t nround = ((size_t)n + 31) / 32 * 32;
   for (size_t i = (size_t)blockIdx.x * SMALL_THREADS + threadIdx.x; i < nround; i += (size_t)gridDim.x * SMALL_THREADS) {
@@ -573,6 +581,111 @@ __global__ void __launch_bounds__(SMALL_THREADS)
     }
   }
   t.flush(&st->next);
+}
+
+// small_call with the tally and the queue counter in `tally` (the
+// cooperative path keeps three of them).
+template <bool kUnique>
+__device__ __forceinline__ void small_activate_t(uint32_t v, Counters *tally, uint32_t *stamp, unsigned level,
+                                                 uint32_t *visited, uint32_t *q_out, const uint32_t *out_deg,
+                                                 const uint32_t *in_deg, Tally &t) {
+  if (!kUnique) {
+    if (stamp[v] == level || atomicExch(stamp + v, level) == level) return;
+  }
+  if (visited) atomicOr(visited + (v >> 5), 1u << (v & 31));
+  uint32_t od = out_deg[v];
+  t.activated += 1;
+  t.edges += od;
+  t.maxdeg = od > t.maxdeg ? od : t.maxdeg;
+  if (in_deg) t.in_edges += in_deg[v];
+  if (od > 0) queue_append_any(v, q_out, &tally->qlen);
+}
+template <class Op, bool kUnique>
+__device__ __forceinline__ void small_call_t(Counters *tally, const uint32_t *__restrict__ q_in,
+                                             uint32_t *__restrict__ q_out, const Dir &d, const Op &op,
+                                             uint32_t *stamp, uint32_t *visited,
+                                             const uint32_t *__restrict__ out_deg,
+                                             const uint32_t *__restrict__ in_deg, uint32_t n, unsigned level) {
+  const unsigned lane = lane_id();
+  Tally t;
+  const size_t nround = ((size_t)n + 31) / 32 * 32;
+  for (size_t i = (size_t)blockIdx.x * SMALL_THREADS + threadIdx.x; i < nround; i += (size_t)gridDim.x * SMALL_THREADS) {
+    const bool valid = i < n;
+    uint32_t src = 0;
+    unsigned long long b = 0, e = 0;
+    if (valid) {
+      src = q_in[i];
+      b = d.off[src];
+      e = d.off[src + 1];
+    }
+    if (valid && e - b <= LIGHT_DEG) {
+      for (unsigned long long k = b; k < e; k++) {
+        uint32_t dst = d.nbr[k];
+        if (op.push(src, (uint32_t)i, dst, d.w ? d.w[k] : 0.0f))
+          small_activate_t<kUnique>(dst, tally, stamp, level, visited, q_out, out_deg, in_deg, t);
+      }
+    }
+    unsigned coop = __ballot_sync(GG_FULL, valid && e - b > LIGHT_DEG);
+    while (coop) {
+      const unsigned leader = __ffs(coop) - 1;
+      coop &= coop - 1;
+      const unsigned long long lb = __shfl_sync(GG_FULL, b, leader), le = __shfl_sync(GG_FULL, e, leader);
+      const uint32_t lsrc = __shfl_sync(GG_FULL, src, leader);
+      const uint32_t li = (uint32_t)__shfl_sync(GG_FULL, (unsigned long long)i, leader);
+      for (unsigned long long k = lb + lane; k < le; k += 32) {
+        uint32_t dst = d.nbr[k];
+        if (op.push(lsrc, li, dst, d.w ? d.w[k] : 0.0f))
+          small_activate_t<kUnique>(dst, tally, stamp, level, visited, q_out, out_deg, in_deg, t);
+      }
+    }
+  }
+  t.flush(tally);
+}
+
+// Closes a small call (one thread, after every block's tally is in): the
+// trace row, the next call's queue and switch value, and whether it runs.
+__device__ __forceinline__ void small_close(SmallRun *st, unsigned long long *tr_ae, unsigned int *tr_act,
+                                            unsigned level) {
+  const unsigned long long ne = atomicAdd(&st->next.edges, 0ull);
+  const unsigned int na = atomicAdd(&st->next.activated, 0u);
+  const unsigned int nq = atomicAdd(&st->next.qlen, 0u);
+  const unsigned int nm = atomicAdd(&st->next.maxdeg, 0u);
+  const unsigned int r = st->calls;
+  tr_ae[r] = st->ae;
+  tr_act[r] = na;
+  st->calls = r + 1;
+  st->total_ae += st->ae;
+  st->level = level + 1;
+  st->ae = ne;
+  st->n = nq;
+  st->last_activated = na;
+  st->next.edges = 0;
+  st->next.in_edges = 0;
+  st->next.activated = 0;
+  st->next.qlen = 0;
+  st->next.maxdeg = 0;
+  st->ticket = 0;
+  st->maxdeg = nm;
+  st->go = (na > 0 && ne < st->edges_lim && nq <= SMALL_MAX_QUEUE && ne <= SMALL_MAX_AE && nm <= SMALL_MAX_DEG)
+               ? 1u
+               : 0u;
+  __threadfence();
+}
+
+template <class Op, bool kUnique>
+__global__ void __launch_bounds__(SMALL_THREADS)
+    push_small(SmallRun *st, const uint32_t *__restrict__ q_in, uint32_t *__restrict__ q_out, Dir d, Op op,
+               uint32_t *stamp, uint32_t *visited, const uint32_t *__restrict__ out_deg,
+               const uint32_t *__restrict__ in_deg, unsigned long long *tr_ae, unsigned int *tr_act) {
+  __shared__ unsigned s_go, s_n, s_level, s_last;
+  if (threadIdx.x == 0) {
+    s_go = st->go;
+    s_n = st->n;
+    s_level = st->level;
+  }
+  __syncthreads();
+  if (!s_go) return;
+  small_call<Op, kUnique>(st, q_in, q_out, d, op, stamp, visited, out_deg, in_deg, s_n, s_level);
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -581,29 +694,57 @@ __global__ void __launch_bounds__(SMALL_THREADS)
   __syncthreads();
   if (s_last && threadIdx.x == 0) {
     __threadfence();
-    const unsigned long long ne = atomicAdd(&st->next.edges, 0ull);
-    const unsigned int na = atomicAdd(&st->next.activated, 0u);
-    const unsigned int nq = atomicAdd(&st->next.qlen, 0u);
-    const unsigned int nm = atomicAdd(&st->next.maxdeg, 0u);
-    const unsigned int r = st->calls;
-    tr_ae[r] = st->ae;
-    tr_act[r] = na;
-    st->calls = r + 1;
-    st->total_ae += st->ae;
-    st->level = level + 1;
-    st->ae = ne;
-    st->n = nq;
+    small_close(st, tr_ae, tr_act, s_level);
+  }
+}
+
+// The same calls in one cooperative launch: up to max_calls of them, the
+// queues alternating (qa -> qb, then qb -> qa, ...), one grid-wide barrier
+// per call.  Call c's tally goes to tally[c % 3]; after the barrier every
+// block reads it and derives the next call's queue length, switch value and
+// whether it runs (identical in all blocks, so all leave the loop together);
+// block 0 writes the trace row and clears tally[(c + 1) % 3], which no block
+// reads any more (the last reads were before the previous barrier).
+template <class Op, bool kUnique>
+__global__ void __launch_bounds__(SMALL_THREADS)
+    push_small_coop(SmallRun *st, Counters *tally, uint32_t *qa, uint32_t *qb, Dir d, Op op, uint32_t *stamp,
+                    uint32_t *visited, const uint32_t *__restrict__ out_deg, const uint32_t *__restrict__ in_deg,
+                    unsigned long long *tr_ae, unsigned int *tr_act, unsigned max_calls) {
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  unsigned n = st->n, level = st->level, go = st->go, maxdeg = st->maxdeg, na = 0;
+  unsigned long long ae = st->ae, total = st->total_ae;
+  const unsigned long long lim = st->edges_lim;
+  unsigned c = 0;
+  for (; c < max_calls && go; c++) {
+    Counters *cur = tally + (c % 3);
+    if (blockIdx.x == 0 && threadIdx.x == 0) memset(tally + ((c + 1) % 3), 0, sizeof(Counters));
+    small_call_t<Op, kUnique>(cur, (c & 1) ? qb : qa, (c & 1) ? qa : qb, d, op, stamp, visited, out_deg, in_deg, n,
+                              level);
+    grid.sync();
+    const unsigned long long ne = *(volatile unsigned long long *)&cur->edges;
+    na = *(volatile unsigned *)&cur->activated;
+    const unsigned nq = *(volatile unsigned *)&cur->qlen;
+    const unsigned nm = *(volatile unsigned *)&cur->maxdeg;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      tr_ae[c] = ae;
+      tr_act[c] = na;
+    }
+    total += ae;
+    level += 1;
+    ae = ne;
+    n = nq;
+    maxdeg = nm;
+    go = (na > 0 && ne < lim && nq <= SMALL_MAX_QUEUE && ne <= SMALL_MAX_AE && nm <= SMALL_MAX_DEG) ? 1u : 0u;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->calls = c;
+    st->total_ae = total;
+    st->level = level;
+    st->ae = ae;
+    st->n = n;
     st->last_activated = na;
-    st->next.edges = 0;
-    st->next.in_edges = 0;
-    st->next.activated = 0;
-    st->next.qlen = 0;
-    st->next.maxdeg = 0;
-    st->ticket = 0;
-    st->maxdeg = nm;
-    st->go = (na > 0 && ne < st->edges_lim && nq <= SMALL_MAX_QUEUE && ne <= SMALL_MAX_AE && nm <= SMALL_MAX_DEG)
-                 ? 1u
-                 : 0u;
+    st->maxdeg = maxdeg;
+    st->go = go;
     __threadfence();
   }
 }
@@ -792,7 +933,9 @@ struct Launch {
     unsigned *tr_act;
     char *blob;
     const size_t st_bytes = 256, ae_bytes = sizeof(unsigned long long) * SMALL_BATCH;
-    GG_TRY(ws(g, WS_SMALL, st_bytes + ae_bytes + sizeof(unsigned) * SMALL_BATCH, &blob));
+    const size_t act_bytes = sizeof(unsigned) * SMALL_BATCH;
+    GG_TRY(ws(g, WS_SMALL, st_bytes + ae_bytes + act_bytes + 3 * sizeof(Counters) + 64, &blob));
+    Counters *coop_tally = (Counters *)(blob + ((st_bytes + ae_bytes + act_bytes + 63) / 64 * 64));
     st = (SmallRun *)blob;
     tr_ae = (unsigned long long *)(blob + st_bytes);
     tr_act = (unsigned *)(blob + st_bytes + ae_bytes);
@@ -823,10 +966,28 @@ struct Launch {
     cudaGraphExec_t exec = nullptr;
     int exec_parity = -1;
     int status = GG_OK;
-    uint32_t batch = 2;
+    // Without message snapshots the calls need no host step between them: one
+    // cooperative launch runs a whole batch (grid = one block per SM, all
+    // resident by the cooperative launch's guarantee) and stops early.
+    const bool coop = !snap_msg && coop_ok();
+    uint32_t batch = coop ? SMALL_BATCH : 2;
     for (;;) {
       cudaError_t e = cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-      if (e == cudaSuccess && batch == SMALL_BATCH) {
+      if (e == cudaSuccess && coop) {
+        uint32_t *qa = q[*cur], *qb = q[*cur ^ 1];
+        Dir dd = d;
+        Op oo = op;
+        const uint32_t *deg = d.deg;
+        unsigned mc = batch;
+        Counters *tally = coop_tally;
+        e = cudaMemsetAsync(tally, 0, sizeof(Counters), s);
+        void *args[] = {&st, &tally, &qa, &qb, &dd, &oo, &stamp, &visited, (void *)&deg, (void *)&in_deg,
+                        &tr_ae, &tr_act, &mc};
+        if (e == cudaSuccess)
+          e = cudaLaunchCooperativeKernel((const void *)push_small_coop<Op, kUnique>, dim3(COOP_BLOCKS),
+                                          dim3(SMALL_THREADS), args, 0, s);
+        launches += 1;
+      } else if (e == cudaSuccess && batch == SMALL_BATCH) {
         if (!exec || exec_parity != *cur) {
           if (exec) cudaGraphExecDestroy(exec);
           exec = nullptr;
@@ -849,7 +1010,7 @@ struct Launch {
         status = cuda_status(e, "small run");
         break;
       }
-      launches += batch * (snap_msg ? 2 : 1);
+      if (!coop) launches += batch * (snap_msg ? 2 : 1);
       status = read_small(g, &h, st, sizeof(h));
       if (status == GG_OK) status = read_small(g, h_ae.data(), tr_ae, sizeof(unsigned long long) * batch);
       if (status == GG_OK) status = read_small(g, h_act.data(), tr_act, sizeof(unsigned) * batch);
@@ -873,6 +1034,11 @@ struct Launch {
     *ae = h.ae;
     *maxdeg = h.maxdeg;
     return GG_OK;
+  }
+  // Cooperative launches available (queried once per device).
+  bool coop_ok() const {
+    int v = 0;
+    return cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, g->device) == cudaSuccess && v;
   }
   static bool small_ok(uint32_t nq, unsigned long long ae, uint32_t maxdeg) {
     return ae > 0 && nq <= SMALL_MAX_QUEUE && ae <= SMALL_MAX_AE && maxdeg <= SMALL_MAX_DEG;

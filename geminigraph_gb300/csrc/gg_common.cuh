@@ -130,6 +130,10 @@ struct gg_graph {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // second stream of the reduction pulls: the light-list kernel runs beside
+  // the chunk kernel (fork / join events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   uint32_t V = 0;
   uint64_t E = 0;
   uint64_t nadj = 0;

@@ -859,8 +859,17 @@ struct Launch {
   template <class Op>
   int pull(const Dir &d, const Op &op, const ActOut &act, Counters *ctr) {
     cudaStream_t s = g->stream;
-    pull_light<Op><<<pull_grid(), PULL_THREADS, 0, s>>>(d, g->V, op, act, ctr);
+    // light lists on the side stream, beside the chunk kernel (disjoint
+    // vertices); the finish, which sets bitmap bits atomically in words the
+    // light kernel stores whole, runs after the join
+    const bool fork = d.nbig && g->side;
+    if (fork) {
+      GG_CUDA(cudaEventRecord(g->fork, s));
+      GG_CUDA(cudaStreamWaitEvent(g->side, g->fork, 0));
+    }
+    pull_light<Op><<<pull_grid(), PULL_THREADS, 0, fork ? g->side : s>>>(d, g->V, op, act, ctr);
     launches += 1;
+    if (fork) GG_CUDA(cudaEventRecord(g->join, g->side));
     if (d.nbig) {
       typename Op::Acc *part = nullptr;
       GG_TRY(ws(g, WS_PARTIAL, d.nbigchunks, &part));
@@ -880,6 +889,7 @@ struct Launch {
         else
           pull_chunks<Op, 8, false><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
       }
+      if (fork) GG_CUDA(cudaStreamWaitEvent(s, g->join, 0));
       pull_big_finish<Op><<<grid_for(d.nbig, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, op, part, act,
                                                                                                   ctr);
       launches += 2;

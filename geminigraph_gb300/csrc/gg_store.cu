@@ -707,6 +707,12 @@ void graph_destroy(gg_graph *g) {
   ws_free_all(g);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->join) cudaEventDestroy(g->join);
+  if (g->side) {
+    cudaStreamSynchronize(g->side);
+    cudaStreamDestroy(g->side);
+  }
   for (cudaEvent_t e : g->evpool) cudaEventDestroy(e);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -732,6 +738,9 @@ static int graph_create(int device, uint32_t V, int weighted, int symmetric, gg_
   cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaMalloc(&g->ws.ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMallocHost(&g->ws.ctr_host, sizeof(Counters));

@@ -1,0 +1,62 @@
+"""The multi-GPU form is replicas only: every rank runs its own graph and
+roots, and ranks meet only for the barrier and the max / sum of the timed
+region (bench.py's Dist over gloo).  These run on the CPU with two ranks."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, port, out):
+    os.environ.update(WORLD_SIZE="2", RANK=str(rank), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    sys.path.insert(0, REPO)
+    import bench
+    d = bench.Dist()
+    d.barrier()
+    mx = d.max(10.0 + rank)
+    sm = d.sum(1.0 + rank)
+    d.barrier()
+    d.close()
+    out.put((rank, mx, sm))
+
+
+def test_dist_two_ranks_gloo():
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=240) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res == [(0, 11.0, 3.0), (1, 11.0, 3.0)]
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """Launched as the scaling run launches it: rank 0 times the reference
+    and prints one line; rank 1 exits 0 without work."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.join(REPO, "bench.py"),
+           "--impl", "reference", "--workload", "pagerank", "--gpus", "2", "--steps", "1", "--warmup", "0"]
+    p = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] in ("reference", "port")

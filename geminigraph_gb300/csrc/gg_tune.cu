@@ -3,7 +3,7 @@
 // load shape (16-byte windows per lane or lane-strided entries).  The best
 // choice depends on the graph's degree distribution, so it is measured on the
 // graph itself: every candidate rebuilds the bins and times, with CUDA
-// events, the objective's workloads: two float PageRank iterations (light
+// events, the objective's workloads: four float PageRank iterations (light
 // and chunked pulls), one BFS from the vertex of largest out-degree (push,
 // pull, small runs) and one 64-root batched BFS (and SSSP on a weighted
 // graph); the
@@ -145,14 +145,14 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     }
     if (roots.empty()) roots.push_back(root);
   }
-  const uint32_t lights[] = {16, 32, 64};
+  const uint32_t lights[] = {16, 32, 64, 128, 256, 512};
   const uint32_t chunks[] = {128, 256, 512};
   auto measure = [&](double *ms) -> int {
     gg_run_stats st;
     memset(&st, 0, sizeof(st));
     double t = 0;
     if (objective & GG_TUNE_PAGERANK) {
-      GG_TRY(gg_pagerank_f32(g, 2, nullptr, nullptr, &st));
+      GG_TRY(gg_pagerank_f32(g, 4, nullptr, nullptr, &st));
       t += st.device_ms;
     }
     if (objective & GG_TUNE_BFS) {

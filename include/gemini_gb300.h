@@ -277,8 +277,8 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
  * lanes load 16-byte windows of the list (pull_vector = 1) or every 32nd
  * entry (0).  gg_graph_set_bins sets all three (light_deg 1..2048;
  * pull_chunk 128, 256 or 512; pull_vector 0 or 1).  gg_autotune times the
- * 18 candidates on the graph itself with CUDA events, on the workloads the
- * objective mask names (GG_TUNE_PAGERANK: two float PageRank iterations;
+ * 36 candidates (light_deg 16 to 512) on the graph itself with CUDA events, on the workloads the
+ * objective mask names (GG_TUNE_PAGERANK: four float PageRank iterations;
  * GG_TUNE_BFS: one BFS; GG_TUNE_BATCHED: one 64-root gg_bfs_batched, and
  * gg_sssp_batched on a weighted graph), keeps the fastest and records it in
  * <cache_dir>/bins_v2.txt (cache_dir NULL: $GG_TUNE_CACHE, else

@@ -429,9 +429,14 @@ def gpu_arm(args, dist):
     ach = per_mode[dom][1] / (per_mode[dom][0] / 1000.0) / 1e9 if per_mode[dom][0] > 0 else 0.0
     traffic = committed_traffic(kname, args.workload, w["scale"])
     total_kernel_ms = per_mode[0][0] + per_mode[1][0]
+    avg_ms = per_mode[dom][0] / max(per_mode[dom][2], 1)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": traffic, "launches": per_mode[dom][2],
+                "traffic": traffic,
+                # DRAM bytes the kernel class really moves (committed ncu capture) over its time:
+                # below frac where pull-mode BFS skips counted edges
+                "dram_frac": round(traffic / (avg_ms / 1000.0) / 1e9 / peak, 4) if traffic and avg_ms > 0 else None,
+                "launches": per_mode[dom][2],
                 "avg_launch_ms": round(per_mode[dom][0] / max(per_mode[dom][2], 1), 4),
                 "share_of_edge_kernel_time": round(per_mode[dom][0] / total_kernel_ms, 4) if total_kernel_ms else None}
     # ---- e2e through the C ABI with host buffers

@@ -431,49 +431,51 @@ static __global__ void __launch_bounds__(PULL_THREADS)
 
 // partials[c] = edge index of the chunk's first active in-neighbour, or ~0.
 static __global__ void __launch_bounds__(PULL_THREADS)
-    bfs_heavy_partial(Dir d, const uint32_t *__restrict__ active_in, const uint32_t *__restrict__ visited,
-                      unsigned long long *__restrict__ partials) {
-  __shared__ unsigned long long s_first;
-  for (uint32_t c = blockIdx.x; c < d.nchunks; c += gridDim.x) {
-    uint32_t h = d.chunk_owner[c];
-    uint32_t v = d.heavy[h];
-    if (threadIdx.x == 0) s_first = ~0ull;
-    __syncthreads();
-    if (!bm_test(visited, v)) {
-      unsigned long long b = d.off[v] + (unsigned long long)(c - d.heavy_chunk[h]) * HEAVY_CHUNK;
-      unsigned long long end = d.off[v + 1];
-      unsigned long long e = b + HEAVY_CHUNK < end ? b + HEAVY_CHUNK : end;
-      for (unsigned long long base = b; base < e; base += PULL_THREADS) {
-        unsigned long long k = base + threadIdx.x;
-        bool hit = k < e && bm_test_ldg(active_in, d.nbr[k]);
-        if (hit) atomicMin(&s_first, k);
-        if (__syncthreads_or(hit)) break;
+    bfs_heavy_first(Dir d, const uint32_t *__restrict__ active_in, const uint32_t *__restrict__ visited,
+                    unsigned long long *first) {
+  // one warp per HEAVY_CHUNK-entry chunk of a list longer than HEAVY_DEG;
+  // first[h] = the lowest hit index of heavy vertex h, so a chunk starting
+  // past it (or a vertex already visited) is skipped and a scan stops at it
+  const size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  const unsigned lane = lane_id();
+  for (size_t c = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); c < d.nchunks; c += nwarps) {
+    const uint32_t h = d.chunk_owner[c];
+    const uint32_t v = d.heavy[h];
+    if (bm_test(visited, v)) continue;
+    const unsigned long long b = d.off[v] + (unsigned long long)(c - d.heavy_chunk[h]) * HEAVY_CHUNK;
+    const unsigned long long end = d.off[v + 1];
+    const unsigned long long e = b + HEAVY_CHUNK < end ? b + HEAVY_CHUNK : end;
+    for (unsigned long long base = b; base < e; base += 32) {
+      unsigned long long best = 0;
+      if (lane == 0) best = *(volatile unsigned long long *)(first + h);
+      if (__shfl_sync(GG_FULL, best, 0) < base) break;
+      const unsigned long long k = base + lane;
+      const bool hit = k < e && bm_test_ldg(active_in, d.nbr[k]);
+      const unsigned bal = __ballot_sync(GG_FULL, hit);
+      if (bal) {
+        if (lane == 0) atomicMin(first + h, base + (unsigned long long)(__ffs(bal) - 1));
+        break;
       }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) partials[c] = s_first;
-    __syncthreads();
   }
 }
 
 static __global__ void __launch_bounds__(PULL_THREADS)
-    bfs_heavy_finish(Dir d, const unsigned long long *__restrict__ partials, uint32_t *parent, ActOut act,
+    bfs_heavy_finish(Dir d, const unsigned long long *__restrict__ first, uint32_t *parent, ActOut act,
                      Counters *ctr) {
   Tally t;
-  size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
-  unsigned lane = lane_id();
-  for (size_t h = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); h < d.nheavy; h += nwarps) {
-    uint32_t v = d.heavy[h];
-    unsigned long long first = ~0ull;
-    if (!bm_test(act.visited, v)) {
-      for (uint32_t c = d.heavy_chunk[h] + lane; c < d.heavy_chunk[h + 1]; c += 32) {
-        unsigned long long p = partials[c];
-        first = p < first ? p : first;
+  const size_t n = ((size_t)d.nheavy + 31) / 32 * 32;
+  for (size_t h = (size_t)blockIdx.x * blockDim.x + threadIdx.x; h < n; h += (size_t)gridDim.x * blockDim.x) {
+    bool a = false;
+    uint32_t v = 0;
+    if (h < d.nheavy) {
+      v = d.heavy[h];
+      const unsigned long long f = first[h];
+      if (f != ~0ull && !bm_test(act.visited, v)) {
+        parent[v] = d.nbr[f];
+        a = true;
       }
-      first = warp_min(first);
     }
-    bool a = lane == 0 && first != ~0ull;
-    if (a) parent[v] = d.nbr[first];
     push_activate(a, v, act, t);
   }
   t.flush(ctr);
@@ -850,10 +852,7 @@ struct Launch {
     return grid_for((size_t)d.nmed * 32, PULL_THREADS, g->num_sms, 8);
   }
   unsigned heavy_grid(const Dir &d) const {
-    return grid_for((size_t)d.nchunks * PULL_THREADS, PULL_THREADS, g->num_sms, 8);
-  }
-  unsigned heavy_finish_grid(const Dir &d) const {
-    return grid_for((size_t)d.nheavy * 32, PULL_THREADS, g->num_sms, 8);
+    return grid_for((size_t)d.nchunks * 32, PULL_THREADS, g->num_sms, 8);
   }
   // All bins of one dense call, in order: light, medium, heavy chunks, heavy finish.
   template <class Op>
@@ -906,10 +905,12 @@ struct Launch {
       launches += 1;
     }
     if (d.nheavy) {
-      unsigned long long *part = nullptr;
-      GG_TRY(ws(g, WS_PARTIAL, d.nchunks, &part));
-      bfs_heavy_partial<<<heavy_grid(d), PULL_THREADS, 0, s>>>(d, active_in, act.visited, part);
-      bfs_heavy_finish<<<heavy_finish_grid(d), PULL_THREADS, 0, s>>>(d, part, parent, act, ctr);
+      unsigned long long *first = nullptr;
+      GG_TRY(ws(g, WS_PARTIAL, d.nheavy, &first));
+      GG_CUDA(cudaMemsetAsync(first, 0xff, sizeof(unsigned long long) * d.nheavy, s));
+      bfs_heavy_first<<<heavy_grid(d), PULL_THREADS, 0, s>>>(d, active_in, act.visited, first);
+      bfs_heavy_finish<<<grid_for(d.nheavy, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, first, parent,
+                                                                                                act, ctr);
       launches += 2;
     }
     GG_CUDA(cudaGetLastError());

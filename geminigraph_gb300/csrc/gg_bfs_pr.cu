@@ -11,7 +11,12 @@ namespace gg {
 struct BfsPush {
   uint32_t *parent;
   uint32_t V;
+  // visited bits are set right after a vertex's parent: most already-reached
+  // targets are turned away by this L2-resident bitmap, not by a random read
+  // of the parent array; parent (then the CAS) stays the authority
+  const uint32_t *visited;
   __device__ __forceinline__ bool push(uint32_t src, uint32_t, uint32_t dst, float) const {
+    if (visited && bm_test(visited, dst)) return false;
     if (*(volatile uint32_t *)(parent + dst) != V) return false;
     return atomicCAS(parent + dst, V, src) == V;
   }
@@ -68,7 +73,7 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
     bool sparse = ae < g->E / 20;
     if (sparse && qvalid && Launch::small_ok(nq, ae, md)) {
       // consecutive small sparse calls run on the device without host round trips
-      GG_TRY((L.small_run<BfsPush, true, uint32_t>(g->out, BfsPush{parent, V}, q, &cur, &nq, &ae, &md, &n_act, visited,
+      GG_TRY((L.small_run<BfsPush, true, uint32_t>(g->out, BfsPush{parent, V, visited}, q, &cur, &nq, &ae, &md, &n_act, visited,
                                                    nullptr, nullptr, nullptr, tr, nullptr)));
       if (n_act > 0) {  // the next call is dense or large: its active set is q[cur]
         GG_CUDA(cudaMemsetAsync(bm[cur], 0, words * 4, s));
@@ -94,7 +99,7 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
         unsigned long long *P;
         GG_TRY(L.scan_queue_degrees(q[cur], nq, g->out.deg, &P));
         GG_TRY(tr.kbegin());
-        push_lb<BfsPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[cur], P, nq, ae, g->out, BfsPush{parent, V},
+        push_lb<BfsPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[cur], P, nq, ae, g->out, BfsPush{parent, V, visited},
                                                                     a, ctr);
         GG_TRY(tr.kend());
         L.launches += 1;

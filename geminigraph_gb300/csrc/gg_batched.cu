@@ -88,6 +88,56 @@ __device__ __forceinline__ void ms_record(uint32_t v, u64 bits, uint32_t u, uint
   }
 }
 
+// Levels of newly reached lanes, written a 256-byte row at a time: each lane
+// of the warp holds a vertex v with its new lanes m and out-degree dg; for
+// every vertex with lanes, thread t writes lvl[v][t] and lvl[v][t + 32] where
+// set and adds them to its per-lane sums (reached, out-degree).
+struct LaneSums {
+  u64 c0 = 0, c1 = 0, e0 = 0, e1 = 0;
+  // all threads of the block call it (shared-memory reduction, then one
+  // atomic per lane and block)
+  __device__ __forceinline__ void flush(u64 *lane_sum) {
+    __shared__ u64 s_sum[2 * LANES];
+    for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x) s_sum[i] = 0;
+    __syncthreads();
+    const unsigned lane = lane_id();
+    if (c0) {
+      atomicAdd(&s_sum[lane], c0);
+      atomicAdd(&s_sum[LANES + lane], e0);
+    }
+    if (c1) {
+      atomicAdd(&s_sum[lane + 32], c1);
+      atomicAdd(&s_sum[LANES + lane + 32], e1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x)
+      if (s_sum[i]) atomicAdd(lane_sum + i, s_sum[i]);
+  }
+};
+__device__ __forceinline__ void mark_rows_warp(uint32_t v, u64 m, uint32_t dg, uint32_t *lvl, uint32_t iter,
+                                               LaneSums &ls) {
+  const unsigned lane = lane_id();
+  unsigned bal = __ballot_sync(GG_FULL, m != 0);
+  while (bal) {
+    const int j = __ffs(bal) - 1;
+    bal &= bal - 1;
+    const uint32_t vj = __shfl_sync(GG_FULL, v, j);
+    const unsigned lo = __shfl_sync(GG_FULL, (unsigned)m, j), hi = __shfl_sync(GG_FULL, (unsigned)(m >> 32), j);
+    const uint32_t dj = __shfl_sync(GG_FULL, dg, j);
+    uint32_t *row = lvl + (size_t)vj * LANES;
+    if ((lo >> lane) & 1u) {
+      row[lane] = iter;
+      ls.c0 += 1;
+      ls.e0 += dj;
+    }
+    if ((hi >> lane) & 1u) {
+      row[lane + 32] = iter;
+      ls.c1 += 1;
+      ls.e1 += dj;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- BFS pull
 // Light lists (<= LIGHT_DEG): the lane's own vertex, in CSC order, so each
 // lane bit takes the first in-neighbour that has it (as bfs.cpp:63-66 does for
@@ -95,9 +145,11 @@ __device__ __forceinline__ void ms_record(uint32_t v, u64 bits, uint32_t u, uint
 // chunk kernel then ORs into).
 __global__ void __launch_bounds__(256)
     ms_pull_light(Dir d, uint32_t V, u64 alive, const u64 *__restrict__ front, u64 *visit, u64 *next, uint32_t *lvl,
-                  uint32_t *par, uint32_t iter, const uint32_t *__restrict__ out_deg, MsCounters *mc) {
+                  uint32_t *par, uint32_t iter, const uint32_t *__restrict__ out_deg, MsCounters *mc,
+                  u64 *lane_sum) {
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
+  LaneSums ls;
   for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < ((size_t)V + 255) / 256 * 256;
        v += (size_t)gridDim.x * blockDim.x) {
     u64 acc = 0;
@@ -134,8 +186,12 @@ __global__ void __launch_bounds__(256)
         t_touched += 1;
       }
     }
+    // levels of this warp's 32 vertices (without parents; long lists are
+    // marked by ms_big_finish)
+    if (lane_sum) mark_rows_warp((uint32_t)v, acc, acc ? out_deg[v] : 0u, lvl, iter, ls);
   }
   ms_flush(mc, t_alive, t_edges, t_touched);
+  if (lane_sum) ls.flush(lane_sum);
 }
 
 // Long lists: one warp per PULL_CHUNK-edge chunk; a lane bit goes to the
@@ -211,65 +267,20 @@ __global__ void __launch_bounds__(256)
     if (s_sum[i]) atomicAdd(lane_sum + i, s_sum[i]);
 }
 
-// Levels of a step without parents: lvl[v][l] = iter for every lane bit of
-// next[v], one 256-byte row per vertex written by a warp (thread t: lanes t
-// and t + 32) instead of one scattered store per bit; the same pass adds the
-// newly reached vertices and their out-degrees to the per-lane sums.
-__global__ void __launch_bounds__(256)
-    ms_mark_levels(uint32_t V, const u64 *__restrict__ next, uint32_t *lvl, uint32_t iter,
-                   const uint32_t *__restrict__ out_deg, u64 *lane_sum) {
-  __shared__ u64 s_sum[2 * LANES];
-  for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x) s_sum[i] = 0;
-  __syncthreads();
-  const size_t nwarps = (size_t)gridDim.x * 8;
-  const unsigned lane = lane_id();
-  u64 c0 = 0, c1 = 0, e0 = 0, e1 = 0;
-  for (size_t g = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g * 32 < V; g += nwarps) {
-    const size_t v = g * 32 + lane;
-    const u64 m = v < V ? next[v] : 0ull;
-    const uint32_t dg = m ? out_deg[v] : 0u;
-    unsigned bal = __ballot_sync(GG_FULL, m != 0);
-    while (bal) {
-      const int j = __ffs(bal) - 1;
-      bal &= bal - 1;
-      const unsigned lo = __shfl_sync(GG_FULL, (unsigned)m, j), hi = __shfl_sync(GG_FULL, (unsigned)(m >> 32), j);
-      const uint32_t dj = __shfl_sync(GG_FULL, dg, j);
-      uint32_t *row = lvl + (g * 32 + j) * LANES;
-      if ((lo >> lane) & 1u) {
-        row[lane] = iter;
-        c0 += 1;
-        e0 += dj;
-      }
-      if ((hi >> lane) & 1u) {
-        row[lane + 32] = iter;
-        c1 += 1;
-        e1 += dj;
-      }
-    }
-  }
-  if (c0) {
-    atomicAdd(&s_sum[lane], c0);
-    atomicAdd(&s_sum[LANES + lane], e0);
-  }
-  if (c1) {
-    atomicAdd(&s_sum[lane + 32], c1);
-    atomicAdd(&s_sum[LANES + lane + 32], e1);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x)
-    if (s_sum[i]) atomicAdd(lane_sum + i, s_sum[i]);
-}
 
 // visit |= next for the long-list vertices, and their tallies.
 __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg,
-                              MsCounters *mc) {
+                              MsCounters *mc, uint32_t *lvl, uint32_t iter, u64 *lane_sum) {
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
+  LaneSums ls;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ((size_t)d.nbig + 255) / 256 * 256;
        i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t v = 0;
+    u64 nx = 0;
     if (i < d.nbig) {
-      const uint32_t v = d.big[i];
-      const u64 nx = next[v];
+      v = d.big[i];
+      nx = next[v];
       if (nx) {
         visit[v] |= nx;
         t_alive |= nx;
@@ -277,8 +288,10 @@ __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, c
         t_touched += 1;
       }
     }
+    if (lane_sum) mark_rows_warp(v, nx, nx ? out_deg[v] : 0u, lvl, iter, ls);
   }
   ms_flush(mc, t_alive, t_edges, t_touched);
+  if (lane_sum) ls.flush(lane_sum);
 }
 
 // ---------------------------------------------------------------- BFS push
@@ -902,19 +915,16 @@ int LanePool::bfs_step() {
   } else {
     if (tr_) GG_TRY(tr_->kbegin());
     ms_pull_light<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-        g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_, g_->out.deg, mc_);
+        g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_, g_->out.deg, mc_, par_ ? nullptr : lane_sum_);
     launches += 1;
     if (g_->in.nbig) {
       ms_pull_chunks<<<grid_for((size_t)g_->in.nbigchunks * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
           g_->in, active_, front_, visit_, next_, lvl_, par_, iter_);
-      ms_big_finish<<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_);
+      ms_big_finish<<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_,
+                                                                            lvl_, iter_, par_ ? nullptr : lane_sum_);
       launches += 2;
     }
-    if (!par_) {
-      ms_mark_levels<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-          V, next_, lvl_, iter_, g_->out.deg, lane_sum_);
-      launches += 1;
-    }
+
     if (tr_) GG_TRY(tr_->kend());
     GG_TRY(read_counters(&h));
     qvalid_ = false;

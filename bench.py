@@ -74,6 +74,9 @@ WORKLOADS = {
     "sssp_batched": dict(kind="rmat", scale=24, ef=16, weighted=True, symmetric=False,
                          desc="batched SSSP, 64 seeded roots per launch, on R-MAT scale 24, edge factor 16, "
                               "float weights in [0,1)"),
+    "build": dict(kind="rmat", scale=26, ef=16, weighted=False, symmetric=False,
+                  desc="graph build (CSR + CSC) of directed R-MAT scale 26, edge factor 16, from records in pinned "
+                       "host memory, partitioned under a device-memory budget"),
 }
 REF_APP = {"bfs": "bfs", "cc": "cc", "pagerank": "pagerank", "pagerank_f64": "pagerank", "sssp": "sssp", "bc": "bc", "bfs_grid": "bfs",
            "bfs_batched": "bfs", "sssp_batched": "sssp", "bc_batched": "bc", "serve": "bfs"}
@@ -215,12 +218,32 @@ def algorithmic_bytes(mode, ae, V, n_frontier, workload):
     return per_edge * ae + n_frontier * (8 + 4 + 4)   # push: frontier offsets, degree, queue entry
 
 
-def make_graph(gg, w, device):
+def make_graph(gg, w, device, **build):
+    """build: build_budget / adjacency_host / force_partitions (gg_build_options)."""
     if w["kind"] == "rmat":
         return gg.Graph.generate(gg.RMAT, w["scale"], w["ef"], SEED, weighted=w["weighted"],
-                                 symmetric=w["symmetric"], device=device)
+                                 symmetric=w["symmetric"], device=device, **build)
     return gg.Graph.generate(gg.GRID, w["scale"], 0, SEED, weighted=w["weighted"], symmetric=w["symmetric"],
-                             device=device)
+                             device=device, **build)
+
+
+def link_h2d_gbs(device, nbytes=1 << 30, reps=5):
+    """Pinned host -> device copy rate (NVLink-C2C on GB300), CUDA events."""
+    import torch
+    src = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dst = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{device}")
+    dst.copy_(src, non_blocking=True)
+    torch.cuda.synchronize(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        dst.copy_(src, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize(device)
+    gbs = nbytes * reps / (e0.elapsed_time(e1) / 1000.0) / 1e9
+    del src, dst
+    torch.cuda.empty_cache()
+    return gbs
 
 
 def run_once(gg, g, workload, arg, to_host, stats_cls):
@@ -343,6 +366,10 @@ def cpu_reference(gg, workload, nsteps, warmup):
 def reference_arm(args, dist):
     if dist.rank != 0:
         return 0
+    if args.workload == "build":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's loader reports no load time of its "
+                          "own (its toolkits time compute() only)"}), flush=True)
+        return 0
     import geminigraph_gb300 as gg
     w = WORKLOADS[args.workload]
     r = cpu_reference(gg, args.workload, args.steps, args.warmup)
@@ -384,7 +411,8 @@ def gpu_arm(args, dist):
     w = WORKLOADS[args.workload]
     device = dist.local_rank
     t0 = time.perf_counter()
-    g = make_graph(gg, w, device)
+    g = make_graph(gg, w, device, build_budget=int(args.build_budget_gb * 1e9),
+                   adjacency_host=args.adjacency == "host")
     build_s = time.perf_counter() - t0
     bins = tune_bins(g, args)
     info = g.info()
@@ -413,7 +441,8 @@ def gpu_arm(args, dist):
     edges_all = dist.sum(edges)
     value = edges_all / t_max / 1e9
     # ---- dominant kernel roofline
-    per_mode = {0: [0.0, 0.0, 0], 1: [0.0, 0.0, 0]}   # ms, bytes, launches
+    per_mode = {0: [0.0, 0.0, 0, 0], 1: [0.0, 0.0, 0, 0]}   # ms, bytes, launches, adjacency bytes
+    adj_per_edge = 8 if w["weighted"] else 4
     for s in stats:
         prev_act = 1
         for i, (mode, ae, act) in enumerate(s.rows()):
@@ -422,6 +451,7 @@ def gpu_arm(args, dist):
             per_mode[mode][0] += ms
             per_mode[mode][1] += algorithmic_bytes(mode, ae, V, frontier, args.workload)
             per_mode[mode][2] += 1
+            per_mode[mode][3] += adj_per_edge * ae
             prev_act = act
     dom = 1 if per_mode[1][0] >= per_mode[0][0] else 0
     kname = {0: "push_lb", 1: "bfs_pull" if args.workload.startswith("bfs") else "pull_reduce"}[dom]
@@ -481,6 +511,8 @@ def gpu_arm(args, dist):
         "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"],
                    "l2": "inputs larger than L2 (graph %.1f GB)" % (info["device_bytes"] / 1e9),
                    "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
+                   "adjacency": args.adjacency, "build_partitions": g.build["partitions"],
+                   "host_adjacency_gb": round(info["host_bytes"] / 1e9, 2),
                    "active_edges_per_step": edges // max(len(stats), 1), "bins": bins},
         "e2e": dict({"value": round(e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                      "d2h_bytes_per_step": d2h, "ms_per_step": round(e_max * 1000 / args.steps, 3)}, **e2e_extra),
@@ -491,6 +523,15 @@ def gpu_arm(args, dist):
         "wall_s": round(wall, 3),
         "clocks": clk,
     }
+    if args.adjacency == "host":
+        # the adjacency reads cross NVLink-C2C: the same achieved rate against the link
+        # only the neighbour (and weight) arrays cross the link
+        link = link_h2d_gbs(device)
+        adj_rate = per_mode[dom][3] / (per_mode[dom][0] / 1000.0) / 1e9 if per_mode[dom][0] > 0 else 0.0
+        line["roofline"]["link"] = {"achieved": round(adj_rate, 1), "peak": round(link, 1), "unit": "GB/s",
+                                    "frac": round(adj_rate / link, 4),
+                                    "bytes": "adjacency bytes of the counted edges (pull-mode BFS reads fewer)",
+                                    "peak_source": "measured pinned host->device copy (torch, CUDA events)"}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         try:
             r = cpu_reference(gg, args.workload, 5, 1)
@@ -511,7 +552,8 @@ def gpu_arm_batched(args, dist):
     w = WORKLOADS[args.workload]
     device = dist.local_rank
     t0 = time.perf_counter()
-    g = make_graph(gg, w, device)
+    g = make_graph(gg, w, device, build_budget=int(args.build_budget_gb * 1e9),
+                   adjacency_host=args.adjacency == "host")
     build_s = time.perf_counter() - t0
     bins = tune_bins(g, args)
     info = g.info()
@@ -578,6 +620,8 @@ def gpu_arm_batched(args, dist):
         "data": "synthetic (seeded R-MAT generated on the device)",
         "config": {"workload": w["desc"], "vertices": V, "edges": info["edges"], "lanes": lanes,
                    "parallelism": f"replicas x{args.gpus}", "graph_build_s": round(build_s, 2),
+                   "adjacency": args.adjacency, "build_partitions": g.build["partitions"],
+                   "host_adjacency_gb": round(info["host_bytes"] / 1e9, 2),
                    "l2": "inputs larger than L2", "bins": bins},
         "plain": {"value": round(plain_qps, 1), "unit": "queries/s",
                   "what": f"{len(plain_roots)} roots one at a time through the single-root kernels (device time)"},
@@ -593,6 +637,75 @@ def gpu_arm_batched(args, dist):
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
+    return 0
+
+
+def gpu_arm_build(args, dist):
+    """Partitioned build from host records (the out-of-core load) against the
+    in-core build of the same records.  A step is one whole build."""
+    import ctypes
+    import geminigraph_gb300 as gg
+    w = WORKLOADS["build"]
+    device = dist.local_rank
+    L = gg.library()
+    rec_host = gg.generate_records(gg.RMAT, w["scale"], w["ef"], SEED + dist.rank, weighted=w["weighted"])
+    ptr = ctypes.c_void_p()
+    gg._check(L.gg_host_alloc(rec_host.nbytes, ctypes.byref(ptr)))
+    rec = np.ctypeslib.as_array((ctypes.c_uint8 * rec_host.nbytes).from_address(ptr.value))
+    rec[:] = rec_host
+    del rec_host
+    V = 1 << w["scale"]
+    E = rec.nbytes // (12 if w["weighted"] else 8)
+    budget = int((args.build_budget_gb or 4.0) * 1e9)
+
+    def build(**kw):
+        t0 = time.perf_counter()
+        g = gg.Graph.from_records(rec, V, weighted=w["weighted"], symmetric=w["symmetric"], device=device, **kw)
+        dt = time.perf_counter() - t0
+        b = dict(g.build)
+        info = g.info()
+        g.close()
+        return dt, b, info
+
+    for _ in range(args.warmup):
+        build(build_budget=budget)
+    dist.barrier()
+    times, parts, info = [], 0, None
+    for _ in range(args.steps):
+        dt, b, info = build(build_budget=budget)
+        times.append(dt)
+        parts = b["partitions"]
+    t_max = dist.max(sum(times))
+    value = dist.sum(E * len(times)) / t_max / 1e6
+    ic = [build()[0] for _ in range(2)]
+    in_core = E / min(ic) / 1e6
+    # the partitioned build reads the records over the link: degrees, range
+    # counts, and one compaction pass per range, for each of the two directions
+    passes = 2 * (parts + 2)
+    read_gbs = passes * rec.nbytes / (sum(times) / len(times)) / 1e9
+    link = link_h2d_gbs(device)
+    line = {
+        "metric": "graph build rate", "value": round(value, 1), "unit": "Medges/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_max * 1000 / args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded R-MAT records generated on the host)",
+        "config": {"workload": w["desc"], "vertices": V, "edges": E, "records_gb": round(rec.nbytes / 1e9, 2),
+                   "build_budget_gb": round(budget / 1e9, 2), "partitions_per_direction": parts,
+                   "graph_device_gb": round(info["device_bytes"] / 1e9, 2),
+                   "in_core_rate_medges_s": round(in_core, 1), "in_core_s": round(min(ic), 3),
+                   "l2": "records and graph larger than L2", "parallelism": f"replicas x{args.gpus}"},
+        "e2e": {"value": round(value, 1), "unit": "Medges/s", "h2d_bytes_per_step": passes * rec.nbytes,
+                "d2h_bytes_per_step": 0},
+        "roofline": {"bound": "link", "kernel": "oc_scatter / oc_count / oc_degree (records read in place)",
+                     "achieved": round(read_gbs, 1), "peak": round(link, 1), "unit": "GB/s",
+                     "frac": round(read_gbs / link, 4),
+                     "peak_source": "measured pinned host->device copy (torch, CUDA events)", "traffic": None},
+        "gpu_launches": None,
+        "cpu_baseline": {"value": None, "note": "the reference's loader reports no load time of its own"},
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    L.gg_host_free(ptr)
     return 0
 
 
@@ -758,6 +871,11 @@ def main():
     ap.add_argument("--bins", default="autotune", choices=["autotune", "default"],
                     help="degree bins: the autotuner's pick for this graph, or the library defaults")
     ap.add_argument("--scale", type=int, default=None, help="override the workload's R-MAT scale / grid side")
+    ap.add_argument("--adjacency", default="device", choices=["device", "host"],
+                    help="neighbour / weight arrays in device memory or in mapped host memory (NVLink-C2C)")
+    ap.add_argument("--build-budget-gb", type=float, default=0.0,
+                    help="device GB the graph build may use beyond the graph (0 = free memory); "
+                         "a smaller budget selects the partitioned build")
     ap.add_argument("--queries", type=int, default=2000, help="serve: queries in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: mean arrival rate (queries/s)")
     ap.add_argument("--plain", type=int, default=300, help="serve: queries replayed one at a time")
@@ -778,6 +896,8 @@ def main():
             return gpu_arm_batched(args, dist)
         if args.workload == "serve":
             return gpu_arm_serve(args, dist)
+        if args.workload == "build":
+            return gpu_arm_build(args, dist)
         return gpu_arm(args, dist)
     finally:
         dist.close()

@@ -34,7 +34,12 @@ class GeminiError(RuntimeError):
 class _Info(ctypes.Structure):
     _fields_ = [("vertices", ctypes.c_uint32), ("edges", ctypes.c_uint64), ("adj_entries", ctypes.c_uint64),
                 ("weighted", ctypes.c_int32), ("symmetric", ctypes.c_int32), ("transposed", ctypes.c_int32),
-                ("device", ctypes.c_int32), ("device_bytes", ctypes.c_uint64)]
+                ("device", ctypes.c_int32), ("device_bytes", ctypes.c_uint64), ("host_bytes", ctypes.c_uint64)]
+
+
+class _BuildOptions(ctypes.Structure):
+    _fields_ = [("build_budget", ctypes.c_uint64), ("adjacency_host", ctypes.c_int32),
+                ("force_partitions", ctypes.c_int32), ("partitions", ctypes.c_uint32), ("build_ms", ctypes.c_double)]
 
 
 class _Stats(ctypes.Structure):
@@ -61,6 +66,9 @@ def library():
         "gg_graph_load": ([ctypes.c_char_p, u32, i32, i32, i32, pg], i32),
         "gg_graph_from_records": ([vp, u64, u32, i32, i32, i32, pg], i32),
         "gg_graph_from_device_records": ([vp, u64, u32, i32, i32, i32, pg], i32),
+        "gg_graph_load_ex": ([ctypes.c_char_p, u32, i32, i32, i32, ctypes.POINTER(_BuildOptions), pg], i32),
+        "gg_graph_from_records_ex": ([vp, u64, u32, i32, i32, i32, ctypes.POINTER(_BuildOptions), pg], i32),
+        "gg_graph_generate_ex": ([i32, u32, u32, u64, i32, i32, i32, ctypes.POINTER(_BuildOptions), pg], i32),
         "gg_graph_generate": ([i32, u32, u32, u64, i32, i32, i32, pg], i32),
         "gg_generate_count": ([i32, u32, u32], u64),
         "gg_generate_records": ([i32, u32, u32, u64, i32, vp, i32], i32),
@@ -217,30 +225,43 @@ def generate_records(kind, p1, p2, seed, weighted=False, threads=0):
 class Graph:
     """One graph resident on one GPU (Graph<EdgeData>, core/graph.hpp:91)."""
 
-    def __init__(self, handle):
+    def __init__(self, handle, build=None):
         self.h = handle
         self._info = None
+        # {"partitions": ranges per direction (1 = in-core), "build_ms": wall time}
+        self.build = build
 
     # -- construction -------------------------------------------------------
-    @classmethod
-    def load(cls, path, vertices, weighted=False, symmetric=False, device=0):
-        """Graph::load_directed / load_undirected_from_directed."""
-        h = ctypes.c_void_p()
-        _check(library().gg_graph_load(os.fsencode(path), vertices, int(weighted), int(symmetric), device,
-                                       ctypes.byref(h)))
-        return cls(h)
+    @staticmethod
+    def _options(build_budget, adjacency_host, force_partitions):
+        return _BuildOptions(build_budget=int(build_budget), adjacency_host=int(bool(adjacency_host)),
+                             force_partitions=int(force_partitions))
 
     @classmethod
-    def from_records(cls, records, vertices, weighted=False, symmetric=False, device=0):
+    def load(cls, path, vertices, weighted=False, symmetric=False, device=0, build_budget=0, adjacency_host=False,
+             force_partitions=0):
+        """Graph::load_directed / load_undirected_from_directed.  build_budget
+        (device bytes beyond the graph, 0 = automatic), force_partitions and
+        adjacency_host are the gg_build_options of gg_graph_load_ex."""
+        h = ctypes.c_void_p()
+        opt = cls._options(build_budget, adjacency_host, force_partitions)
+        _check(library().gg_graph_load_ex(os.fsencode(path), vertices, int(weighted), int(symmetric), device,
+                                          ctypes.byref(opt), ctypes.byref(h)))
+        return cls(h, {"partitions": opt.partitions, "build_ms": opt.build_ms})
+
+    @classmethod
+    def from_records(cls, records, vertices, weighted=False, symmetric=False, device=0, build_budget=0,
+                     adjacency_host=False, force_partitions=0):
         buf = np.frombuffer(records, np.uint8) if isinstance(records, (bytes, bytearray)) else \
             np.ascontiguousarray(records).view(np.uint8)
         h = ctypes.c_void_p()
-        _check(library().gg_graph_from_records(_ptr(buf), buf.nbytes, vertices, int(weighted), int(symmetric),
-                                               device, ctypes.byref(h)))
-        return cls(h)
+        opt = cls._options(build_budget, adjacency_host, force_partitions)
+        _check(library().gg_graph_from_records_ex(_ptr(buf), buf.nbytes, vertices, int(weighted), int(symmetric),
+                                                  device, ctypes.byref(opt), ctypes.byref(h)))
+        return cls(h, {"partitions": opt.partitions, "build_ms": opt.build_ms})
 
     @classmethod
-    def from_edges(cls, vertices, src, dst, w=None, symmetric=False, device=0):
+    def from_edges(cls, vertices, src, dst, w=None, symmetric=False, device=0, **build):
         n = len(src)
         if w is None:
             rec = np.empty(n, dtype=[("s", "<u4"), ("d", "<u4")])
@@ -249,14 +270,16 @@ class Graph:
             rec["w"] = w
         rec["s"] = src
         rec["d"] = dst
-        return cls.from_records(rec, vertices, weighted=w is not None, symmetric=symmetric, device=device)
+        return cls.from_records(rec, vertices, weighted=w is not None, symmetric=symmetric, device=device, **build)
 
     @classmethod
-    def generate(cls, kind, p1, p2, seed, weighted=False, symmetric=False, device=0):
+    def generate(cls, kind, p1, p2, seed, weighted=False, symmetric=False, device=0, build_budget=0,
+                 adjacency_host=False, force_partitions=0):
         h = ctypes.c_void_p()
-        _check(library().gg_graph_generate(kind, p1, p2, seed, int(weighted), int(symmetric), device,
-                                           ctypes.byref(h)))
-        return cls(h)
+        opt = cls._options(build_budget, adjacency_host, force_partitions)
+        _check(library().gg_graph_generate_ex(kind, p1, p2, seed, int(weighted), int(symmetric), device,
+                                              ctypes.byref(opt), ctypes.byref(h)))
+        return cls(h, {"partitions": opt.partitions, "build_ms": opt.build_ms})
 
     def close(self):
         if self.h:

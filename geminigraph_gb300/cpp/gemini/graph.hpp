@@ -92,10 +92,13 @@ class Graph {
   Graph(const Graph &) = delete;
   Graph &operator=(const Graph &) = delete;
 
-  // core/graph.hpp:772
-  void load_directed(std::string path, VertexId n) { load(path, n, false); }
+  // core/graph.hpp:772.  opt (may be null): device-memory budget of the build,
+  // partitioned build, adjacency in host memory (gg_build_options).
+  void load_directed(std::string path, VertexId n, gg_build_options *opt = nullptr) { load(path, n, false, opt); }
   // core/graph.hpp:350
-  void load_undirected_from_directed(std::string path, VertexId n) { load(path, n, true); }
+  void load_undirected_from_directed(std::string path, VertexId n, gg_build_options *opt = nullptr) {
+    load(path, n, true, opt);
+  }
 
   // core/graph.hpp:760
   void transpose() {
@@ -160,9 +163,9 @@ class Graph {
   gg_graph *handle() const { return g_; }
 
  private:
-  void load(const std::string &path, VertexId n, bool sym) {
+  void load(const std::string &path, VertexId n, bool sym, gg_build_options *opt) {
     const int weighted = std::is_same<EdgeData, float>::value ? 1 : 0;
-    gemini::check(gg_graph_load(path.c_str(), n, weighted, sym ? 1 : 0, device_, &g_), "load");
+    gemini::check(gg_graph_load_ex(path.c_str(), n, weighted, sym ? 1 : 0, device_, opt, &g_), "load");
     gg_graph_info info;
     gemini::check(gg_graph_info_get(g_, &info), "info");
     vertices = info.vertices;

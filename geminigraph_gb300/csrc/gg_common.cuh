@@ -141,6 +141,10 @@ struct gg_graph {
   gg::Dir out, in;
   gg::Workspace ws;
   uint64_t graph_bytes = 0;
+  // neighbour and weight arrays in mapped pinned host memory (kernels read
+  // them over NVLink-C2C); offsets, degrees and bins stay in device memory
+  int adj_host = 0;
+  uint64_t host_bytes = 0;
   int num_sms = 0;
   const void *result[2] = {nullptr, nullptr};
   std::vector<cudaEvent_t> evpool;  // events for per-call kernel timing

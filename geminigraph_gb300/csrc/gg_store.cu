@@ -17,6 +17,8 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <algorithm>
+#include <chrono>
 #include <thread>
 #include <vector>
 
@@ -511,9 +513,42 @@ int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk, uint32_t vec) {
   return GG_OK;
 }
 
+// Neighbour / weight storage: device memory, or mapped pinned host memory
+// when the graph keeps its adjacency on the host (the kernels dereference
+// the same pointer over NVLink-C2C; unified addressing makes the host and
+// device addresses of a mapped allocation equal).
+static int adj_alloc(gg_graph *g, bool host, void **p, size_t bytes) {
+  *p = nullptr;
+  if (!host) {
+    GG_CUDA(cudaMalloc(p, bytes));
+    g->graph_bytes += bytes;
+    return GG_OK;
+  }
+  GG_CUDA(cudaHostAlloc(p, bytes, cudaHostAllocMapped));
+  void *dp = nullptr;
+  cudaError_t e = cudaHostGetDevicePointer(&dp, *p, 0);
+  if (e != cudaSuccess || dp != *p) {
+    cudaFreeHost(*p);
+    *p = nullptr;
+    if (e != cudaSuccess) return cuda_status(e, "mapped adjacency");
+    set_error("mapped host adjacency needs unified addressing");
+    return GG_ERR_CUDA;
+  }
+  g->host_bytes += bytes;
+  return GG_OK;
+}
+
+static void adj_release(bool host, void *p) {
+  if (!p) return;
+  if (host)
+    cudaFreeHost(p);
+  else
+    cudaFree(p);
+}
+
 // Builds one direction from keys already written by make_keys.
 static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_alt, uint32_t *v_alt, size_t n,
-                     int bits, Dir *d, bool weights = true) {
+                     int bits, Dir *d, bool weights = true, bool host = false) {
   uint64_t *ks;
   uint32_t *vs;
   GG_TRY(radix_sort(g, keys, vals, k_alt, v_alt, n, 2 * bits, &ks, &vs));
@@ -522,10 +557,10 @@ static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_al
   // padded to a multiple of 64 entries: chunked pulls load whole aligned
   // 16-byte windows that may run past the last list
   const size_t npad = (n + 64) / 64 * 64;
-  GG_CUDA(cudaMalloc(&d->nbr, sizeof(uint32_t) * npad));
+  GG_TRY(adj_alloc(g, host, (void **)&d->nbr, sizeof(uint32_t) * npad));
   GG_CUDA(cudaMemsetAsync(d->nbr + n, 0, sizeof(uint32_t) * (npad - n), g->stream));
   GG_CUDA(cudaMalloc(&d->deg, sizeof(uint32_t) * ((size_t)V + 1)));
-  g->graph_bytes += sizeof(uint64_t) * ((size_t)V + 1) + sizeof(uint32_t) * (npad + (size_t)V + 1);
+  g->graph_bytes += sizeof(uint64_t) * ((size_t)V + 1) + sizeof(uint32_t) * ((size_t)V + 1);
   if (n == 0) {
     GG_CUDA(cudaMemsetAsync(d->off, 0, sizeof(uint64_t) * ((size_t)V + 1), g->stream));
   } else {
@@ -535,9 +570,8 @@ static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_al
   degrees_from_offsets<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->off, V, d->deg);
   GG_CUDA(cudaGetLastError());
   if (g->weighted && weights) {
-    GG_CUDA(cudaMalloc(&d->w, sizeof(float) * (n ? n : 1)));
-    g->graph_bytes += sizeof(float) * n;
-    if (n) GG_CUDA(cudaMemcpyAsync(d->w, vs, sizeof(float) * n, cudaMemcpyDeviceToDevice, g->stream));
+    GG_TRY(adj_alloc(g, host, (void **)&d->w, sizeof(float) * (n ? n : 1)));
+    if (n) GG_CUDA(cudaMemcpyAsync(d->w, vs, sizeof(float) * n, cudaMemcpyDefault, g->stream));
   }
   size_t words = bitmap_words32(V);
   GG_CUDA(cudaMalloc(&d->nz, sizeof(uint32_t) * words));
@@ -548,10 +582,10 @@ static int build_dir(gg_graph *g, uint64_t *keys, uint32_t *vals, uint64_t *k_al
   return GG_OK;
 }
 
-static void free_dir(Dir *d) {
+static void free_dir(Dir *d, bool adj_host) {
   if (d->off) cudaFree(d->off);
-  if (d->nbr) cudaFree(d->nbr);
-  if (d->w) cudaFree(d->w);
+  adj_release(adj_host, d->nbr);
+  adj_release(adj_host, d->w);
   if (d->deg) cudaFree(d->deg);
   if (d->nz) cudaFree(d->nz);
   if (d->med) cudaFree(d->med);
@@ -702,8 +736,8 @@ void graph_destroy(gg_graph *g) {
   pools_destroy(g);
   pr_layout_free(g);
   bool alias = g->in.nbr == g->out.nbr;
-  free_dir(&g->out);
-  if (!alias) free_dir(&g->in);
+  free_dir(&g->out, g->adj_host);
+  if (!alias) free_dir(&g->in, g->adj_host);
   ws_free_all(g);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
@@ -799,7 +833,7 @@ static int build_from_device_records(gg_graph *g, const uint32_t *rec, uint64_t 
         break;
       }
     }
-    status = build_dir(g, k0, v0, k1, v1, n, bits, pass == 0 ? &g->out : &g->in);
+    status = build_dir(g, k0, v0, k1, v1, n, bits, pass == 0 ? &g->out : &g->in, true, g->adj_host != 0);
   }
   cudaStreamSynchronize(g->stream);
   cudaFree(k0);
@@ -809,6 +843,395 @@ static int build_from_device_records(gg_graph *g, const uint32_t *rec, uint64_t 
   if (err) cudaFree(err);
   if (status == GG_OK && g->symmetric) g->in = g->out;
   return status;
+}
+
+// ------------------------------------------------------- partitioned build
+// core/graph.hpp:805-821 streams the edge file in CHUNKSIZE pieces so the
+// whole edge list is never resident at once.  The partitioned build keeps
+// the records where they are (host memory, pinned or registered for the
+// build, read by the kernels over NVLink-C2C; or device memory) and builds
+// each direction in ranges of its major ids: one pass counts degrees (the
+// offsets), one pass counts the entries of every (range, tile) pair, then per
+// range a stable, tile-ordered compaction of its entries, the in-core build's
+// stable radix sort on the range-relative key, and a copy into the range's
+// slice of the final arrays.  Both builds sort stably on (major, minor) from
+// the same entry order (records forward, then reversed for symmetric
+// graphs), so the adjacency, weights included, is identical.  Device memory
+// beyond the graph itself is bounded by the largest range's sort buffers.
+
+constexpr int OC_THREADS = 256;
+constexpr int OC_TILE = 4096;                     // entries per block
+constexpr int OC_WARP = OC_TILE / (OC_THREADS / 32);  // 512 consecutive entries per warp
+constexpr int OC_ROUNDS = OC_WARP / 32;           // 16
+// Greedy ranges of at most cap entries: two neighbouring ranges together hold
+// more than cap (else they would be one), so n entries make at most
+// 2n/cap + 1 ranges; 1024 covers every forced count up to 256.
+constexpr uint32_t OC_MAX_PARTS = 1024;
+constexpr int32_t OC_MAX_FORCED = 256;
+
+// Entry j of the build order.  mode 0: major = src; 1: major = dst;
+// 2 (symmetric): j < E forward, j >= E record j - E reversed.
+struct EntrySrc {
+  const uint32_t *rec;
+  uint64_t E;
+  int words;
+  int mode;
+  __device__ __forceinline__ void ids(uint64_t j, uint32_t &maj, uint32_t &mnr) const {
+    const bool rev = j >= E;
+    const uint64_t r = rev ? j - E : j;
+    const uint32_t s = rec[r * words], d = rec[r * words + 1];
+    const bool swap = mode == 1 || (mode == 2 && rev);
+    maj = swap ? d : s;
+    mnr = swap ? s : d;
+  }
+  __device__ __forceinline__ uint32_t weight_bits(uint64_t j) const {
+    const uint64_t r = j >= E ? j - E : j;
+    return words == 3 ? rec[r * words + 2] : 0u;
+  }
+};
+
+__global__ void oc_degree(EntrySrc src, uint64_t nv, uint32_t V, uint32_t *__restrict__ cnt, unsigned *err) {
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nv; j += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t maj, mnr;
+    src.ids(j, maj, mnr);
+    if (maj >= V || mnr >= V) {
+      atomicOr(err, 1u);
+      continue;
+    }
+    atomicAdd(&cnt[maj], 1u);
+  }
+}
+
+struct U32AsU64 {
+  const uint32_t *p;
+  __device__ __forceinline__ uint64_t operator()(size_t i) const { return p[i]; }
+};
+
+// One thread: greedy ranges [bounds[k], bounds[k+1]) of at most cap entries
+// (a single longer list is a range of its own).  *nparts = 0 when more than
+// max_parts ranges would be needed.
+__global__ void oc_bounds(const uint64_t *__restrict__ off, uint32_t V, uint64_t cap, uint32_t max_parts,
+                          uint32_t *__restrict__ bounds, uint64_t *__restrict__ base, uint32_t *nparts) {
+  if (blockIdx.x || threadIdx.x) return;
+  uint32_t a = 0, k = 0;
+  bounds[0] = 0;
+  base[0] = 0;
+  while (a < V) {
+    if (k == max_parts) {
+      *nparts = 0;
+      return;
+    }
+    const uint64_t lim = off[a] + cap;
+    uint32_t lo = a + 1, hi = V;
+    if (off[lo] > lim) {
+      hi = lo;
+    } else {
+      while (lo < hi) {  // largest b in [a+1, V] with off[b] <= lim
+        const uint32_t mid = lo + (hi - lo + 1) / 2;
+        if (off[mid] <= lim)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+    }
+    k++;
+    bounds[k] = hi;
+    base[k] = off[hi];
+    a = hi;
+  }
+  *nparts = k;
+}
+
+__device__ __forceinline__ uint32_t oc_part_of(const uint32_t *sb, uint32_t nparts, uint32_t maj) {
+  uint32_t lo = 0, hi = nparts - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) / 2;
+    if (sb[mid] <= maj)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// counts[p * ntiles + t] = entries of tile t whose major id lies in range p.
+__global__ void __launch_bounds__(OC_THREADS) oc_count(EntrySrc src, uint64_t nv, const uint32_t *__restrict__ bounds,
+                                                       uint32_t nparts, uint32_t ntiles, uint32_t *__restrict__ counts) {
+  __shared__ uint32_t sb[OC_MAX_PARTS + 1];
+  __shared__ uint32_t hist[OC_MAX_PARTS];
+  for (uint32_t i = threadIdx.x; i <= nparts; i += OC_THREADS) sb[i] = bounds[i];
+  for (uint32_t i = threadIdx.x; i < nparts; i += OC_THREADS) hist[i] = 0;
+  __syncthreads();
+  const uint64_t base = (uint64_t)blockIdx.x * OC_TILE;
+  for (int r = 0; r < OC_TILE / OC_THREADS; r++) {
+    const uint64_t j = base + (uint64_t)r * OC_THREADS + threadIdx.x;
+    if (j < nv) {
+      uint32_t maj, mnr;
+      src.ids(j, maj, mnr);
+      atomicAdd(&hist[oc_part_of(sb, nparts, maj)], 1u);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < nparts; i += OC_THREADS) counts[(size_t)i * ntiles + blockIdx.x] = hist[i];
+}
+
+// Entries of range p = [lo, hi) in build order: warp w of tile t owns
+// entries [t*4096 + w*512, +512), written after the earlier tiles' and
+// warps' entries of the range.  Keys are (major - lo, minor); writes past
+// cap (records changed under the build) are dropped.
+__global__ void __launch_bounds__(OC_THREADS) oc_scatter(EntrySrc src, uint64_t nv, uint32_t lo, uint32_t hi,
+                                                         int bits, const uint32_t *__restrict__ scanned,
+                                                         const uint32_t *__restrict__ counts, uint32_t ntiles,
+                                                         uint32_t p, uint64_t cap, uint64_t *__restrict__ keys,
+                                                         uint32_t *__restrict__ vals) {
+  if (counts[(size_t)p * ntiles + blockIdx.x] == 0) return;
+  __shared__ uint32_t wcnt[OC_THREADS / 32];
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const uint64_t base = (uint64_t)blockIdx.x * OC_TILE + (uint64_t)w * OC_WARP;
+  uint32_t maj[OC_ROUNDS], mnr[OC_ROUNDS];
+  unsigned in_mask = 0, total = 0;
+#pragma unroll
+  for (int r = 0; r < OC_ROUNDS; r++) {
+    const uint64_t j = base + (uint64_t)r * 32 + lane;
+    bool in = false;
+    maj[r] = mnr[r] = 0;
+    if (j < nv) {
+      src.ids(j, maj[r], mnr[r]);
+      in = maj[r] >= lo && maj[r] < hi;
+    }
+    in_mask |= (unsigned)in << r;
+    total += __popc(__ballot_sync(GG_FULL, in));
+  }
+  if (lane == 0) wcnt[w] = total;
+  __syncthreads();
+  uint64_t pos = scanned[(size_t)p * ntiles + blockIdx.x] - scanned[(size_t)p * ntiles];
+  for (unsigned ww = 0; ww < w; ww++) pos += wcnt[ww];
+#pragma unroll
+  for (int r = 0; r < OC_ROUNDS; r++) {
+    const bool in = (in_mask >> r) & 1u;
+    const unsigned b = __ballot_sync(GG_FULL, in);
+    if (in) {
+      const uint64_t at = pos + __popc(b & lanemask_lt());
+      if (at < cap) {
+        keys[at] = ((uint64_t)(maj[r] - lo) << bits) | mnr[r];
+        if (vals) vals[at] = src.weight_bits(base + (uint64_t)r * 32 + lane);
+      }
+    }
+    pos += __popc(b);
+  }
+}
+
+__global__ void oc_emit(const uint64_t *__restrict__ ks, const uint32_t *__restrict__ vs, uint64_t n, int bits,
+                        uint32_t *__restrict__ nbr, uint32_t *__restrict__ w) {
+  const uint64_t mask = (1ull << bits) - 1;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    nbr[i] = (uint32_t)(ks[i] & mask);
+    if (w) w[i] = vs[i];
+  }
+}
+
+// Device buffers freed together when the build returns.
+struct DevScratch {
+  std::vector<void *> p;
+  DevScratch() = default;
+  DevScratch(const DevScratch &) = delete;
+  DevScratch &operator=(const DevScratch &) = delete;
+  ~DevScratch() {
+    for (void *q : p) cudaFree(q);
+  }
+  template <typename T>
+  int get(T **out, size_t count) {
+    void *q = nullptr;
+    GG_CUDA(cudaMalloc(&q, count ? count * sizeof(T) : 16));
+    p.push_back(q);
+    *out = (T *)q;
+    return GG_OK;
+  }
+};
+
+// Sort-buffer bytes per entry of a range: two key buffers, two value
+// buffers when weighted, the radix sort's per-tile digit counts.
+static uint64_t oc_entry_bytes(int weighted) { return 16 + (weighted ? 8 : 0) + 1; }
+
+// One direction by ranges of at most cap entries (force_parts > 0: at least
+// that many ranges).  rec is readable by the device.
+static int build_dir_partitioned(gg_graph *g, const uint32_t *rec, uint64_t E, int mode, Dir *d, uint64_t cap,
+                                 uint32_t force_parts, uint32_t *parts_out) {
+  const uint32_t V = g->V;
+  const int words = g->weighted ? 3 : 2;
+  const uint64_t n = mode == 2 ? 2 * E : E;
+  const int bits = bits_for(V);
+  const bool host = g->adj_host != 0;
+  EntrySrc src{rec, E, words, mode};
+  GG_CUDA(cudaMalloc(&d->off, sizeof(uint64_t) * ((size_t)V + 1)));
+  GG_CUDA(cudaMalloc(&d->deg, sizeof(uint32_t) * ((size_t)V + 1)));
+  g->graph_bytes += sizeof(uint64_t) * ((size_t)V + 1) + sizeof(uint32_t) * ((size_t)V + 1);
+  const size_t npad = (n + 64) / 64 * 64;
+  GG_TRY(adj_alloc(g, host, (void **)&d->nbr, sizeof(uint32_t) * npad));
+  GG_CUDA(cudaMemsetAsync(d->nbr + n, 0, sizeof(uint32_t) * (npad - n), g->stream));
+  if (g->weighted) GG_TRY(adj_alloc(g, host, (void **)&d->w, sizeof(float) * (n ? n : 1)));
+
+  // degrees -> offsets
+  DevScratch tmp;
+  unsigned *err = nullptr;
+  uint64_t *scan64 = nullptr;
+  uint32_t *bounds = nullptr, *nparts_dev = nullptr;
+  uint64_t *base_dev = nullptr;
+  GG_TRY(tmp.get(&err, 1));
+  GG_TRY(tmp.get(&scan64, scan_scratch_elems(V) + 1));
+  GG_TRY(tmp.get(&bounds, OC_MAX_PARTS + 1));
+  GG_TRY(tmp.get(&base_dev, OC_MAX_PARTS + 1));
+  GG_TRY(tmp.get(&nparts_dev, 1));
+  GG_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), g->stream));
+  GG_CUDA(cudaMemsetAsync(d->deg, 0, sizeof(uint32_t) * ((size_t)V + 1), g->stream));
+  if (n) {
+    oc_degree<<<grid_for(n, 256, g->num_sms, 16), 256, 0, g->stream>>>(src, n, V, d->deg, err);
+    GG_CUDA(cudaGetLastError());
+  }
+  unsigned herr = 0;
+  GG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  if (herr) {
+    set_error("an edge names a vertex id >= vertices (%u)", V);
+    return GG_ERR_RANGE;
+  }
+  GG_CUDA((exclusive_scan<uint64_t, U32AsU64>(U32AsU64{d->deg}, V, d->off, scan64, g->stream, nullptr)));
+
+  // ranges
+  if (force_parts) cap = (n + force_parts - 1) / force_parts;
+  if (cap == 0) cap = 1;
+  oc_bounds<<<1, 1, 0, g->stream>>>(d->off, V, cap, OC_MAX_PARTS, bounds, base_dev, nparts_dev);
+  GG_CUDA(cudaGetLastError());
+  uint32_t nparts = 0;
+  GG_CUDA(cudaMemcpyAsync(&nparts, nparts_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  if (nparts == 0) {
+    set_error("build budget too small: more than %u ranges of %llu entries per direction", OC_MAX_PARTS,
+              (unsigned long long)cap);
+    return GG_ERR_NOMEM;
+  }
+  std::vector<uint32_t> hb(nparts + 1);
+  std::vector<uint64_t> hbase(nparts + 1);
+  GG_CUDA(cudaMemcpy(hb.data(), bounds, sizeof(uint32_t) * (nparts + 1), cudaMemcpyDeviceToHost));
+  GG_CUDA(cudaMemcpy(hbase.data(), base_dev, sizeof(uint64_t) * (nparts + 1), cudaMemcpyDeviceToHost));
+  uint64_t maxnp = 0;
+  for (uint32_t p = 0; p < nparts; p++) maxnp = std::max<uint64_t>(maxnp, hbase[p + 1] - hbase[p]);
+  *parts_out = nparts;
+
+  if (n) {
+    const uint64_t ntiles64 = (n + OC_TILE - 1) / OC_TILE;
+    const uint32_t ntiles = (uint32_t)ntiles64;
+    const size_t ncounts = (size_t)nparts * ntiles;
+    uint32_t *counts = nullptr, *scanned = nullptr, *scan32 = nullptr;
+    GG_TRY(tmp.get(&counts, ncounts));
+    GG_TRY(tmp.get(&scanned, ncounts + 1));
+    GG_TRY(tmp.get(&scan32, scan_scratch_elems(ncounts) + 1));
+    oc_count<<<ntiles, OC_THREADS, 0, g->stream>>>(src, n, bounds, nparts, ntiles, counts);
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA((exclusive_scan<uint32_t, ArrayIn<uint32_t>>(ArrayIn<uint32_t>{counts}, ncounts, scanned, scan32,
+                                                         g->stream, nullptr)));
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint32_t *v0 = nullptr, *v1 = nullptr;
+    GG_TRY(tmp.get(&k0, maxnp));
+    GG_TRY(tmp.get(&k1, maxnp));
+    if (g->weighted) {
+      GG_TRY(tmp.get(&v0, maxnp));
+      GG_TRY(tmp.get(&v1, maxnp));
+    }
+    for (uint32_t p = 0; p < nparts; p++) {
+      const uint64_t np = hbase[p + 1] - hbase[p];
+      if (np == 0) continue;
+      const uint32_t lo = hb[p], hi = hb[p + 1];
+      oc_scatter<<<ntiles, OC_THREADS, 0, g->stream>>>(src, n, lo, hi, bits, scanned, counts, ntiles, p, np, k0,
+                                                       v0);
+      GG_CUDA(cudaGetLastError());
+      uint64_t *ks;
+      uint32_t *vs;
+      GG_TRY(radix_sort(g, k0, v0, k1, v1, np, bits + bits_for(hi - lo), &ks, &vs));
+      oc_emit<<<grid_for(np, 256, g->num_sms, 16), 256, 0, g->stream>>>(ks, vs, np, bits, d->nbr + hbase[p],
+                                                                       d->w ? (uint32_t *)d->w + hbase[p] : nullptr);
+      GG_CUDA(cudaGetLastError());
+    }
+  }
+  degrees_from_offsets<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->off, V, d->deg);
+  GG_CUDA(cudaGetLastError());
+  size_t words32 = bitmap_words32(V);
+  GG_CUDA(cudaMalloc(&d->nz, sizeof(uint32_t) * words32));
+  g->graph_bytes += sizeof(uint32_t) * words32;
+  nonzero_bitmap<<<grid_for(words32 * 32, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->deg, V, d->nz, words32);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  GG_TRY(build_bins(g, d));
+  return GG_OK;
+}
+
+// Device bytes of the built graph (both directions, bins estimated at
+// 12 B per vertex), without the adjacency when it lives on the host.
+static uint64_t graph_estimate(uint32_t V, uint64_t n, int weighted, int symmetric, int adj_host) {
+  const uint64_t npad = (n + 64) / 64 * 64;
+  uint64_t per_dir = ((uint64_t)V + 1) * 12 + (uint64_t)V / 8 + (uint64_t)V * 12;
+  if (!adj_host) per_dir += npad * 4 + (weighted ? n * 4 : 0);
+  return per_dir * (symmetric ? 1 : 2);
+}
+
+// Chooses the build: in-core when its working set (records copied to the
+// device unless already there, two key and value buffers, radix counts) fits
+// the budget, else ranges of cap entries.  budget 0: free device memory less
+// the graph and a reserve.
+static int build_plan(gg_graph *g, uint64_t E, bool rec_on_device, const gg_build_options *opt, bool *partitioned,
+                      uint64_t *cap) {
+  const uint64_t n = g->symmetric ? 2 * E : E;
+  const uint64_t unit = g->weighted ? 12 : 8;
+  const uint64_t in_core = (rec_on_device ? 0 : E * unit) + n * oc_entry_bytes(g->weighted);
+  uint64_t budget = opt ? opt->build_budget : 0;
+  if (budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    GG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const uint64_t graph = graph_estimate(g->V, n, g->weighted, g->symmetric, g->adj_host);
+    const uint64_t reserve = ((uint64_t)1 << 30) + total_b / 32;
+    budget = free_b > graph + reserve ? free_b - graph - reserve : 0;
+  }
+  const bool force = opt && opt->force_partitions > 0;
+  *partitioned = force || in_core > budget;
+  *cap = 0;
+  if (!*partitioned) return GG_OK;
+  if (force) return GG_OK;
+  // range buffers + (range, tile) counts (room for 64 ranges) + the offsets scan
+  const uint64_t tiles = (n + OC_TILE - 1) / OC_TILE;
+  const uint64_t fixed = (uint64_t)g->V * 8 + tiles * 8 * 64 + (64ull << 20);
+  const uint64_t per = oc_entry_bytes(g->weighted);
+  *cap = budget > fixed ? (budget - fixed) / per : 0;
+  if (*cap < (1ull << 16) && *cap < n) {
+    set_error("build needs %llu device bytes beyond the graph; %llu available", (unsigned long long)in_core,
+              (unsigned long long)budget);
+    return GG_ERR_NOMEM;
+  }
+  return GG_OK;
+}
+
+// Builds both directions from E records readable by the device at rec.
+static int build_records(gg_graph *g, const uint32_t *rec, uint64_t E, bool partitioned, uint64_t cap,
+                         gg_build_options *opt) {
+  if (opt) opt->partitions = 1;
+  if (!partitioned) return build_from_device_records(g, rec, E);
+  g->E = E;
+  const uint64_t n = g->symmetric ? 2 * E : E;
+  g->nadj = n;
+  if (n >= 0xFFFFFFFFull) {
+    set_error("%llu adjacency entries per direction: the device sort supports < 2^32", (unsigned long long)n);
+    return GG_ERR_TOO_LARGE;
+  }
+  const uint32_t force = opt && opt->force_partitions > 0 ? (uint32_t)opt->force_partitions : 0;
+  uint32_t parts = 0;
+  for (int pass = 0; pass < (g->symmetric ? 1 : 2); pass++) {
+    const int mode = g->symmetric ? 2 : pass;
+    uint32_t pp = 0;
+    GG_TRY(build_dir_partitioned(g, rec, E, mode, pass == 0 ? &g->out : &g->in, cap, force, &pp));
+    parts = std::max(parts, pp);
+  }
+  if (g->symmetric) g->in = g->out;
+  if (opt) opt->partitions = parts;
+  return GG_OK;
 }
 
 static uint64_t unit_of(int weighted) { return weighted ? 12 : 8; }
@@ -921,7 +1344,11 @@ int gg_graph_from_device_records(const void *d_records, uint64_t bytes, uint32_t
   }
   gg_graph *g = nullptr;
   GG_TRY(graph_create(device, vertices, weighted, symmetric, &g));
-  int s = build_from_device_records(g, (const uint32_t *)d_records, bytes / unit_of(weighted));
+  const uint64_t E = bytes / unit_of(weighted);
+  bool part = false;
+  uint64_t cap = 0;
+  int s = build_plan(g, E, true, nullptr, &part, &cap);
+  if (s == GG_OK) s = build_records(g, (const uint32_t *)d_records, E, part, cap, nullptr);
   if (s != GG_OK) {
     graph_destroy(g);
     return s;
@@ -930,30 +1357,158 @@ int gg_graph_from_device_records(const void *d_records, uint64_t bytes, uint32_t
   return GG_OK;
 }
 
-int gg_graph_from_records(const void *records, uint64_t bytes, uint32_t vertices, int weighted, int symmetric,
-                          int device, gg_graph **out) {
+// Device-readable view of host records for the partitioned build: device
+// or pinned memory as it is, anything else registered for the call.
+struct RecordsView {
+  const uint32_t *dev = nullptr;
+  void *registered = nullptr;
+  void *staged = nullptr;  // pinned copy when the range cannot be registered
+  RecordsView() = default;
+  RecordsView(const RecordsView &) = delete;
+  RecordsView &operator=(const RecordsView &) = delete;
+  ~RecordsView() {
+    if (registered) cudaHostUnregister(registered);
+    if (staged) cudaFreeHost(staged);
+  }
+};
+
+static int records_view(const void *records, uint64_t bytes, RecordsView *rv) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, records) != cudaSuccess) {
+    cudaGetLastError();
+    a.type = cudaMemoryTypeUnregistered;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+    rv->dev = (const uint32_t *)records;
+    return GG_OK;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    rv->dev = (const uint32_t *)a.devicePointer;
+    return GG_OK;
+  }
+  void *p = const_cast<void *>(records);
+  cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped | cudaHostRegisterReadOnly);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaHostRegister(p, bytes, cudaHostRegisterMapped);
+  }
+  void *dp = nullptr;
+  if (e == cudaSuccess) {
+    rv->registered = p;
+    GG_CUDA(cudaHostGetDevicePointer(&dp, p, 0));
+  } else {
+    // e.g. the range shares pages with memory registered elsewhere
+    cudaGetLastError();
+    GG_CUDA(cudaHostAlloc(&rv->staged, bytes, cudaHostAllocMapped));
+    memcpy(rv->staged, records, bytes);
+    GG_CUDA(cudaHostGetDevicePointer(&dp, rv->staged, 0));
+  }
+  rv->dev = (const uint32_t *)dp;
+  return GG_OK;
+}
+
+static double wall_ms_since(const std::chrono::steady_clock::time_point &t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+static int graph_create_opts(int device, uint32_t V, int weighted, int symmetric, const gg_build_options *opt,
+                             gg_graph **out) {
+  GG_TRY(graph_create(device, V, weighted, symmetric, out));
+  if (opt && opt->adjacency_host) {
+    (*out)->adj_host = 1;
+    (*out)->pr_layout = 0;
+  }
+  if (opt && (opt->force_partitions < 0 || opt->force_partitions > OC_MAX_FORCED)) {
+    graph_destroy(*out);
+    *out = nullptr;
+    set_error("force_partitions must be in [0, %d]", OC_MAX_FORCED);
+    return GG_ERR_INVALID;
+  }
+  return GG_OK;
+}
+
+int gg_graph_from_records_ex(const void *records, uint64_t bytes, uint32_t vertices, int weighted, int symmetric,
+                             int device, gg_build_options *opt, gg_graph **out) {
+  const auto t0 = std::chrono::steady_clock::now();
   uint64_t unit = unit_of(weighted);
   uint64_t E = bytes / unit;
   if (!out || (!records && E)) {
     set_error("null argument");
     return GG_ERR_INVALID;
   }
+  if ((uintptr_t)records % 4) {
+    set_error("records must be 4-byte aligned");
+    return GG_ERR_INVALID;
+  }
   gg_graph *g = nullptr;
-  GG_TRY(graph_create(device, vertices, weighted, symmetric, &g));
-  void *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, E * unit ? E * unit : 16);
-  if (e == cudaSuccess && E) e = cudaMemcpy(d, records, E * unit, cudaMemcpyHostToDevice);
-  int s = e == cudaSuccess ? build_from_device_records(g, (const uint32_t *)d, E) : cuda_status(e, "copy records");
-  if (d) cudaFree(d);
+  GG_TRY(graph_create_opts(device, vertices, weighted, symmetric, opt, &g));
+  bool part = false;
+  uint64_t cap = 0;
+  int s = build_plan(g, E, false, opt, &part, &cap);
+  if (s == GG_OK && !part) {
+    void *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, E * unit ? E * unit : 16);
+    if (e == cudaSuccess && E) e = cudaMemcpy(d, records, E * unit, cudaMemcpyDefault);
+    s = e == cudaSuccess ? build_records(g, (const uint32_t *)d, E, false, 0, opt) : cuda_status(e, "copy records");
+    if (d) cudaFree(d);
+  } else if (s == GG_OK) {
+    RecordsView rv;
+    s = E ? records_view(records, E * unit, &rv) : GG_OK;
+    if (s == GG_OK) s = build_records(g, rv.dev, E, true, cap, opt);
+    cudaStreamSynchronize(g->stream);
+  }
   if (s != GG_OK) {
     graph_destroy(g);
     return s;
   }
+  if (opt) opt->build_ms = wall_ms_since(t0);
   *out = g;
   return GG_OK;
 }
 
+int gg_graph_from_records(const void *records, uint64_t bytes, uint32_t vertices, int weighted, int symmetric,
+                          int device, gg_graph **out) {
+  return gg_graph_from_records_ex(records, bytes, vertices, weighted, symmetric, device, nullptr, out);
+}
+
+// Reads [0, bytes) of fd into dst with several threads.
+static int read_parallel(int fd, char *dst, uint64_t bytes, const char *path) {
+  const int T = 8;
+  const uint64_t per = (bytes / T + 4095) / 4096 * 4096;
+  std::vector<std::thread> th;
+  std::vector<int> bad(T, 0);
+  for (int t = 0; t < T; t++) {
+    const uint64_t a = per * t, b = std::min<uint64_t>(bytes, per * (t + 1));
+    if (a >= b) break;
+    th.emplace_back([=, &bad]() {
+      uint64_t off = a;
+      while (off < b) {
+        const size_t want = (size_t)std::min<uint64_t>(b - off, (uint64_t)1 << 30);
+        ssize_t r = pread(fd, dst + off, want, (off_t)off);
+        if (r <= 0) {
+          bad[t] = 1;
+          return;
+        }
+        off += (uint64_t)r;
+      }
+    });
+  }
+  for (auto &x : th) x.join();
+  for (int t = 0; t < T; t++)
+    if (bad[t]) {
+      set_error("read error on %s", path);
+      return GG_ERR_IO;
+    }
+  return GG_OK;
+}
+
 int gg_graph_load(const char *path, uint32_t vertices, int weighted, int symmetric, int device, gg_graph **out) {
+  return gg_graph_load_ex(path, vertices, weighted, symmetric, device, nullptr, out);
+}
+
+int gg_graph_load_ex(const char *path, uint32_t vertices, int weighted, int symmetric, int device,
+                     gg_build_options *opt, gg_graph **out) {
+  const auto t0 = std::chrono::steady_clock::now();
   if (!path || !out) {
     set_error("null argument");
     return GG_ERR_INVALID;
@@ -973,9 +1528,40 @@ int gg_graph_load(const char *path, uint32_t vertices, int weighted, int symmetr
   uint64_t E = (uint64_t)st.st_size / unit;
   uint64_t total = E * unit;
   gg_graph *g = nullptr;
-  int s = graph_create(device, vertices, weighted, symmetric, &g);
+  int s = graph_create_opts(device, vertices, weighted, symmetric, opt, &g);
   if (s != GG_OK) {
     close(fd);
+    return s;
+  }
+  bool part = false;
+  uint64_t cap = 0;
+  s = build_plan(g, E, false, opt, &part, &cap);
+  if (s == GG_OK && part) {
+    // records stay in mapped pinned host memory, read by the build kernels
+    char *h = nullptr;
+    cudaError_t e = cudaHostAlloc((void **)&h, total ? total : 16, cudaHostAllocMapped);
+    if (e != cudaSuccess) s = cuda_status(e, "pinned records");
+    if (s == GG_OK) s = read_parallel(fd, h, total, path);
+    close(fd);
+    void *dp = nullptr;
+    if (s == GG_OK) {
+      e = cudaHostGetDevicePointer(&dp, h, 0);
+      if (e != cudaSuccess) s = cuda_status(e, "pinned records");
+    }
+    if (s == GG_OK) s = build_records(g, (const uint32_t *)dp, E, true, cap, opt);
+    cudaStreamSynchronize(g->stream);
+    if (h) cudaFreeHost(h);
+    if (s != GG_OK) {
+      graph_destroy(g);
+      return s;
+    }
+    if (opt) opt->build_ms = wall_ms_since(t0);
+    *out = g;
+    return GG_OK;
+  }
+  if (s != GG_OK) {
+    close(fd);
+    graph_destroy(g);
     return s;
   }
   // stream the file through two pinned chunks
@@ -1024,12 +1610,13 @@ int gg_graph_load(const char *path, uint32_t vertices, int weighted, int symmetr
     if (pin[i]) cudaFreeHost(pin[i]);
     if (done[i]) cudaEventDestroy(done[i]);
   }
-  if (s == GG_OK) s = build_from_device_records(g, (const uint32_t *)d, E);
+  if (s == GG_OK) s = build_records(g, (const uint32_t *)d, E, false, 0, opt);
   if (d) cudaFree(d);
   if (s != GG_OK) {
     graph_destroy(g);
     return s;
   }
+  if (opt) opt->build_ms = wall_ms_since(t0);
   *out = g;
   return GG_OK;
 }
@@ -1080,6 +1667,12 @@ int gg_generate_records(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int w
 
 int gg_graph_generate(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted, int symmetric, int device,
                       gg_graph **out) {
+  return gg_graph_generate_ex(kind, p1, p2, seed, weighted, symmetric, device, nullptr, out);
+}
+
+int gg_graph_generate_ex(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted, int symmetric, int device,
+                         gg_build_options *opt, gg_graph **out) {
+  const auto t0 = std::chrono::steady_clock::now();
   uint64_t E = gg_generate_count(kind, p1, p2);
   uint32_t V;
   if (kind == 0 && p1 >= 1 && p1 <= 31) {
@@ -1095,7 +1688,7 @@ int gg_graph_generate(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int wei
     return GG_ERR_INVALID;
   }
   gg_graph *g = nullptr;
-  GG_TRY(graph_create(device, V, weighted, symmetric, &g));
+  GG_TRY(graph_create_opts(device, V, weighted, symmetric, opt, &g));
   uint32_t *d = nullptr;
   int words = weighted ? 3 : 2;
   cudaError_t e = cudaMalloc(&d, E ? E * words * 4 : 16);
@@ -1108,12 +1701,16 @@ int gg_graph_generate(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int wei
       gen_grid_kernel<<<blocks, 256, 0, g->stream>>>(d, E, p1, key, weighted);
     e = cudaGetLastError();
   }
-  int s = e == cudaSuccess ? build_from_device_records(g, d, E) : cuda_status(e, "generate");
+  bool part = false;
+  uint64_t cap = 0;
+  int s = e == cudaSuccess ? build_plan(g, E, true, opt, &part, &cap) : cuda_status(e, "generate");
+  if (s == GG_OK) s = build_records(g, d, E, part, cap, opt);
   if (d) cudaFree(d);
   if (s != GG_OK) {
     graph_destroy(g);
     return s;
   }
+  if (opt) opt->build_ms = wall_ms_since(t0);
   *out = g;
   return GG_OK;
 }
@@ -1138,6 +1735,7 @@ int gg_graph_info_get(const gg_graph *g, gg_graph_info *info) {
   uint64_t ws_bytes = 0;
   for (int i = 0; i < WS_NSLOTS; i++) ws_bytes += g->ws.bytes[i];
   info->device_bytes = g->graph_bytes + ws_bytes;
+  info->host_bytes = g->host_bytes;
   return GG_OK;
 }
 
@@ -1181,9 +1779,9 @@ int gg_graph_adjacency(const gg_graph *g, int incoming, uint64_t *offsets, uint3
   const Dir &d = incoming ? g->in : g->out;
   if (offsets) GG_CUDA(cudaMemcpy(offsets, d.off, sizeof(uint64_t) * ((size_t)g->V + 1), cudaMemcpyDeviceToHost));
   if (neighbours && g->nadj)
-    GG_CUDA(cudaMemcpy(neighbours, d.nbr, sizeof(uint32_t) * g->nadj, cudaMemcpyDeviceToHost));
+    GG_CUDA(cudaMemcpy(neighbours, d.nbr, sizeof(uint32_t) * g->nadj, cudaMemcpyDefault));
   if (weights && g->weighted && g->nadj)
-    GG_CUDA(cudaMemcpy(weights, d.w, sizeof(float) * g->nadj, cudaMemcpyDeviceToHost));
+    GG_CUDA(cudaMemcpy(weights, d.w, sizeof(float) * g->nadj, cudaMemcpyDefault));
   if (degree) GG_CUDA(cudaMemcpy(degree, d.deg, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost));
   return GG_OK;
 }

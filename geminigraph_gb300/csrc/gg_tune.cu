@@ -105,8 +105,9 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   cudaFree(d_h);
   const uint32_t root = hm[1] < g->V ? hm[1] : 0;
   char key[160];
-  snprintf(key, sizeof(key), "%u:%llu:%llu:%d:%d:%u:%016llx", g->V, (unsigned long long)g->E,
-           (unsigned long long)g->nadj, g->weighted, g->symmetric, objective, h);
+  // host-resident adjacency is read over NVLink-C2C: its bins are tuned apart
+  snprintf(key, sizeof(key), "%u:%llu:%llu:%d:%d:%u:%016llx%s", g->V, (unsigned long long)g->E,
+           (unsigned long long)g->nadj, g->weighted, g->symmetric, objective, h, g->adj_host ? ":host" : "");
   gg_tune_result r;
   memset(&r, 0, sizeof(r));
   // cached?

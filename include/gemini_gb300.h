@@ -50,6 +50,7 @@ typedef struct {
   int32_t transposed;        /* 1: after an odd number of gg_graph_transpose calls */
   int32_t device;            /* CUDA device ordinal */
   uint64_t device_bytes;     /* device memory held by the graph and its workspace */
+  uint64_t host_bytes;       /* pinned host memory holding the adjacency (adjacency_host) */
 } gg_graph_info;
 
 /* Per-call record of a traversal: one row per process_edges call. */
@@ -97,11 +98,48 @@ int gg_graph_from_records(const void *records, uint64_t bytes, uint32_t vertices
 int gg_graph_from_device_records(const void *d_records, uint64_t bytes, uint32_t vertices,
                                  int weighted, int symmetric, int device, gg_graph **out);
 
+/* Options of the graph build (core/graph.hpp:805-821 streams the edge file in
+ * CHUNKSIZE pieces so that the whole list is never resident at once; this is
+ * the device-memory form of that bound).  The in-core build holds the records
+ * and two sort buffers on the device (about 3x the adjacency).  When that
+ * working set exceeds the budget, the partitioned build leaves the records in
+ * host memory (pinned, or registered for the duration of the call; the
+ * kernels read them over NVLink-C2C) and builds each direction in ranges of
+ * its major ids, holding one range's sort buffers at a time.  Both builds
+ * give identical adjacency (same neighbour and weight order).
+ * adjacency_host = 1 keeps the neighbour and weight arrays in mapped pinned
+ * host memory, read by every kernel over NVLink-C2C, for graphs larger than
+ * free device memory; PageRank then pulls the plain incoming adjacency (its
+ * renumbered device copy is off unless gg_graph_set_pr_layout asks for it). */
+typedef struct {
+  uint64_t build_budget;     /* in: device bytes the build may hold beyond the graph;
+                                0 = free device memory less the graph and a reserve */
+  int32_t adjacency_host;    /* in: 1 = neighbour / weight arrays in host memory */
+  int32_t force_partitions;  /* in: 1..256 = partitioned build, ranges of at most
+                                ceil(entries / force_partitions) entries (a longer
+                                list is a range of its own); 0 = by budget */
+  uint32_t partitions;       /* out: ranges per direction (1 = in-core build) */
+  double build_ms;           /* out: wall time of the call */
+} gg_build_options;
+
+/* gg_graph_load / gg_graph_from_records with build options (opt may be NULL:
+ * automatic budget, adjacency in device memory).  The plain calls choose the
+ * build the same way. */
+int gg_graph_load_ex(const char *path, uint32_t vertices, int weighted, int symmetric, int device,
+                     gg_build_options *opt, gg_graph **out);
+int gg_graph_from_records_ex(const void *records, uint64_t bytes, uint32_t vertices, int weighted,
+                             int symmetric, int device, gg_build_options *opt, gg_graph **out);
+
 /* Builds a graph from a seeded R-MAT (a=.57 b=.19 c=.19 d=.05) or grid edge list
  * generated on the device; identical to loading the file gg_generate_* writes.
  * kind 0 = R-MAT (p1 = scale, p2 = edge factor), 1 = grid (p1 = side, p2 unused). */
 int gg_graph_generate(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted,
                       int symmetric, int device, gg_graph **out);
+
+/* gg_graph_generate with build options (the records are generated in device
+ * memory; opt may be NULL). */
+int gg_graph_generate_ex(int kind, uint32_t p1, uint32_t p2, uint64_t seed, int weighted, int symmetric,
+                         int device, gg_build_options *opt, gg_graph **out);
 
 /* Host generator of the same records (records = edge count * 8 or 12 bytes). */
 uint64_t gg_generate_count(int kind, uint32_t p1, uint32_t p2);

@@ -680,8 +680,8 @@ def gpu_arm_build(args, dist):
     ic = [build()[0] for _ in range(2)]
     in_core = E / min(ic) / 1e6
     # the partitioned build reads the records over the link: degrees, range
-    # counts, and one compaction pass per range, for each of the two directions
-    passes = 2 * (parts + 2)
+    # counts, and one compaction pass per group of ranges, for each direction
+    passes = b["record_passes"]
     read_gbs = passes * rec.nbytes / (sum(times) / len(times)) / 1e9
     link = link_h2d_gbs(device)
     line = {
@@ -691,6 +691,7 @@ def gpu_arm_build(args, dist):
         "data": "synthetic (seeded R-MAT records generated on the host)",
         "config": {"workload": w["desc"], "vertices": V, "edges": E, "records_gb": round(rec.nbytes / 1e9, 2),
                    "build_budget_gb": round(budget / 1e9, 2), "partitions_per_direction": parts,
+                   "record_passes": passes,
                    "graph_device_gb": round(info["device_bytes"] / 1e9, 2),
                    "in_core_rate_medges_s": round(in_core, 1), "in_core_s": round(min(ic), 3),
                    "l2": "records and graph larger than L2", "parallelism": f"replicas x{args.gpus}"},

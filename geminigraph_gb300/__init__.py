@@ -39,7 +39,8 @@ class _Info(ctypes.Structure):
 
 class _BuildOptions(ctypes.Structure):
     _fields_ = [("build_budget", ctypes.c_uint64), ("adjacency_host", ctypes.c_int32),
-                ("force_partitions", ctypes.c_int32), ("partitions", ctypes.c_uint32), ("build_ms", ctypes.c_double)]
+                ("force_partitions", ctypes.c_int32), ("partitions", ctypes.c_uint32),
+                ("record_passes", ctypes.c_uint32), ("build_ms", ctypes.c_double)]
 
 
 class _Stats(ctypes.Structure):
@@ -247,7 +248,8 @@ class Graph:
         opt = cls._options(build_budget, adjacency_host, force_partitions)
         _check(library().gg_graph_load_ex(os.fsencode(path), vertices, int(weighted), int(symmetric), device,
                                           ctypes.byref(opt), ctypes.byref(h)))
-        return cls(h, {"partitions": opt.partitions, "build_ms": opt.build_ms})
+        return cls(h, {"partitions": opt.partitions, "record_passes": opt.record_passes,
+                       "build_ms": opt.build_ms})
 
     @classmethod
     def from_records(cls, records, vertices, weighted=False, symmetric=False, device=0, build_budget=0,
@@ -258,7 +260,8 @@ class Graph:
         opt = cls._options(build_budget, adjacency_host, force_partitions)
         _check(library().gg_graph_from_records_ex(_ptr(buf), buf.nbytes, vertices, int(weighted), int(symmetric),
                                                   device, ctypes.byref(opt), ctypes.byref(h)))
-        return cls(h, {"partitions": opt.partitions, "build_ms": opt.build_ms})
+        return cls(h, {"partitions": opt.partitions, "record_passes": opt.record_passes,
+                       "build_ms": opt.build_ms})
 
     @classmethod
     def from_edges(cls, vertices, src, dst, w=None, symmetric=False, device=0, **build):
@@ -279,7 +282,8 @@ class Graph:
         opt = cls._options(build_budget, adjacency_host, force_partitions)
         _check(library().gg_graph_generate_ex(kind, p1, p2, seed, int(weighted), int(symmetric), device,
                                               ctypes.byref(opt), ctypes.byref(h)))
-        return cls(h, {"partitions": opt.partitions, "build_ms": opt.build_ms})
+        return cls(h, {"partitions": opt.partitions, "record_passes": opt.record_passes,
+                       "build_ms": opt.build_ms})
 
     def close(self):
         if self.h:

@@ -119,6 +119,8 @@ typedef struct {
                                 ceil(entries / force_partitions) entries (a longer
                                 list is a range of its own); 0 = by budget */
   uint32_t partitions;       /* out: ranges per direction (1 = in-core build) */
+  uint32_t record_passes;    /* out: passes over the records, all directions (partitioned:
+                                degrees, range counts, one per group of ranges) */
   double build_ms;           /* out: wall time of the call */
 } gg_build_options;
 

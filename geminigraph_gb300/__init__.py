@@ -100,6 +100,7 @@ def library():
         "gg_graph_set_bins": ([vp, u32, u32, u32], i32),
         "gg_bfs_many": ([vp, vp, i32, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_sssp_delta": ([vp, ctypes.c_float], i32),
+        "gg_graph_set_batched_switch": ([vp, u32], i32),
         "gg_dump_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
@@ -312,6 +313,9 @@ class Graph:
 
     def set_bins(self, light_deg, pull_chunk, pull_vector=1):
         _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk, 1 if pull_vector else 0))
+
+    def set_batched_switch(self, divisor):
+        _check(library().gg_graph_set_batched_switch(self.h, int(divisor)))
 
     def set_sssp_delta(self, delta):
         _check(library().gg_graph_set_sssp_delta(self.h, float(delta)))

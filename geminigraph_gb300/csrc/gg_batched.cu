@@ -880,7 +880,7 @@ static unsigned push_grid_for(const gg_graph *g, unsigned long long total) {
 
 int LanePool::bfs_step() {
   const uint32_t V = g_->V;
-  const bool sparse = ae_ < g_->E / 20;
+  const bool sparse = ae_ < g_->E / g_->batched_switch_div;
   if (tr_) tr_->add(sparse ? 0 : 1, ae_, 0);
   iter_ += 1;
   LaneCounters h;
@@ -1202,7 +1202,16 @@ extern "C" uint64_t gg_result_checksum(const void *values, uint32_t vertices, in
   return sum;
 }
 
-extern "C" int gg_graph_set_sssp_delta(gg_graph *g, float delta) {
+extern "C" int gg_graph_set_batched_switch(gg_graph *g, uint32_t divisor) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  g->batched_switch_div = divisor ? divisor : 20;
+  return GG_OK;
+}
+
+int gg_graph_set_sssp_delta(gg_graph *g, float delta) {
   if (!g || !(delta >= 0.0f)) {
     gg::set_error("the bucket width must be >= 0");
     return GG_ERR_INVALID;

@@ -162,6 +162,9 @@ struct gg_graph {
   // batched SSSP bucket width (0: plain Bellman-Ford rounds) and the least
   // edge weight (bucketing needs none negative), found on first use
   float sssp_delta = 0.0f;
+  // batched BFS steps pull (dense) when the union frontier's out-edges reach
+  // edges / batched_switch_div, else push
+  uint32_t batched_switch_div = 20;
   int wmin_known = 0;
   float wmin = 0.0f;
 };

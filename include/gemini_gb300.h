@@ -232,6 +232,11 @@ int gg_bfs_batched(gg_graph *g, const uint32_t *roots, int nroots, int32_t *leve
 int gg_sssp_batched(gg_graph *g, const uint32_t *roots, int nroots, float *distances, uint64_t *reached,
                     gg_run_stats *stats);
 
+/* Sparse/dense switch of the batched BFS steps: a step pulls when the union
+ * frontier's out-edges reach edges / divisor (0 = 20, the reference's rule,
+ * core/graph.hpp:1509).  Levels and reached counts do not depend on it. */
+int gg_graph_set_batched_switch(gg_graph *g, uint32_t divisor);
+
 /* Batched SSSP relaxation order (no reference counterpart): delta > 0
  * expands each lane's lowered vertices in rising distance buckets of this
  * width; 0 (the default) runs plain Bellman-Ford rounds, which on R-MAT

@@ -134,3 +134,19 @@ def test_bfs_batched_levels_without_parents(case, n):
         parent, single = g.bfs(r)
         assert np.array_equal(lv[i], bfs_levels(parent, r)), f"lane {i} root {r}"
         assert int(edges[i]) == single.active_edges_total
+
+
+@pytest.mark.parametrize("divisor", [2, 160])
+def test_bfs_batched_switch_point_keeps_levels(case, divisor):
+    """Moving the batched sparse/dense switch changes which kernels run, not
+    the levels or the reached counts."""
+    V, s, d, w, g = case
+    roots = roots_for(V, s, 16, seed=300 + divisor)
+    ref = gg.bfs_batched(g, roots, levels=True, parents=False)
+    g.set_batched_switch(divisor)
+    try:
+        lv, _, reached, _, _ = gg.bfs_batched(g, roots, levels=True, parents=True)
+    finally:
+        g.set_batched_switch(0)
+    assert np.array_equal(lv, ref[0])
+    assert np.array_equal(reached, ref[2])

@@ -815,12 +815,47 @@ def gpu_arm_serve(args, dist):
                 "d2h_bytes_per_step": 16, "note": "per query the root in and reached count + checksum out"},
         "clocks": clk,
     }
+    server.close()
+    if args.mix:
+        line["mix_ceiling"] = serve_mix_ceiling(gg, graphs, degs, scales, probs)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
-    server.close()
     for g in graphs:
         g.close()
     return 0
+
+
+def serve_mix_ceiling(gg, graphs, degs, scales, probs):
+    """Per graph and kind: plain per-query wall time (one gg_bfs / gg_sssp per
+    root) against full 64-root batches, and the serving mix's speed-up if
+    every batch were full (75% BFS / 25% SSSP, the stream's graph weights)."""
+    rows, pl, ba = [], 0.0, 0.0
+    for g, deg, sc, p in zip(graphs, degs, scales, probs):
+        roots = gg.pick_roots(deg, 3 * 64, seed=SEED + 9000 + sc)
+        cost = {}
+        for kind in ("bfs", "sssp"):
+            one = g.bfs if kind == "bfs" else g.sssp
+            for r in roots[:2]:
+                one(int(r), to_host=False)
+            k = 16 if kind == "bfs" or sc < 26 else 6
+            t0 = time.perf_counter()
+            for r in roots[:k]:
+                one(int(r), to_host=False)
+            plain = (time.perf_counter() - t0) / k * 1000
+            batch = (lambda rs: gg.bfs_batched(g, rs, levels=False, parents=False)) if kind == "bfs" else \
+                (lambda rs: gg.sssp_batched(g, rs, distances=False))
+            batch(roots[:64])
+            t0 = time.perf_counter()
+            batch(roots[64:128])
+            batch(roots[128:192])
+            batched = (time.perf_counter() - t0) / 128 * 1000
+            cost[kind] = (plain, batched)
+            rows.append({"scale": sc, "kind": kind, "plain_ms_per_query": round(plain, 3),
+                         "batched_ms_per_query": round(batched, 3), "x": round(plain / batched, 2)})
+        pl += p * (0.75 * cost["bfs"][0] + 0.25 * cost["sssp"][0])
+        ba += p * (0.75 * cost["bfs"][1] + 0.25 * cost["sssp"][1])
+    return {"rows": rows, "plain_ms_per_query": round(pl, 3), "full_batch_ms_per_query": round(ba, 3),
+            "speedup_if_full": round(pl / ba, 2)}
 
 
 def run_once_stats(gg, g, workload, a, st):
@@ -880,6 +915,8 @@ def main():
     ap.add_argument("--queries", type=int, default=2000, help="serve: queries in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: mean arrival rate (queries/s)")
     ap.add_argument("--plain", type=int, default=300, help="serve: queries replayed one at a time")
+    ap.add_argument("--mix", action="store_true",
+                    help="serve: also time plain and full-batch queries per graph and kind (the mix's ceiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")

@@ -28,8 +28,9 @@ struct CcPull {
   using Acc = uint32_t;
   const uint32_t *cur;
   uint32_t *nxt;
+  const uint32_t *ids = nullptr;  // hot-source layout: vertex id of each rank (the message starts at dst's id)
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
-  __device__ __forceinline__ uint32_t identity(uint32_t v) const { return v; }
+  __device__ __forceinline__ uint32_t identity(uint32_t v) const { return ids ? ids[v] : v; }
   __device__ __forceinline__ uint32_t identity_coop() const { return 0xffffffffu; }
   __device__ __forceinline__ uint32_t gather(const Dir &, unsigned long long, uint32_t u) const { return cur[u]; }
   __device__ __forceinline__ uint32_t combine(uint32_t a, uint32_t b) const { return b < a ? b : a; }
@@ -98,9 +99,9 @@ struct SsspPull {
 // activate something, with a message snapshot for push calls and two state
 // buffers for pull calls.
 template <typename T, class PushOp, class PullOp>
-static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
-                      uint32_t n_act, uint32_t nq, uint32_t md, bool qvalid, unsigned long long ae, Trace &tr,
-                      Launch &L, T **result) {
+static int relax_loop(gg_graph *g, const Dir &dout, const Dir &din, const PullOp &pull, T *state0, T *state1,
+                      uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1, uint32_t n_act, uint32_t nq, uint32_t md,
+                      bool qvalid, unsigned long long ae, Trace &tr, Launch &L, T **result) {
   const uint32_t V = g->V;
   const size_t words = bitmap_words32(V);
   cudaStream_t s = g->stream;
@@ -118,35 +119,38 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
     bool sparse = ae < g->E / 20;
     if (sparse && qvalid && Launch::small_ok(nq, ae, md)) {
       // consecutive small sparse calls run on the device without host round trips
-      GG_TRY((L.small_run<PushOp, false, T>(g->out, PushOp{cur, msg}, q, &c_i, &nq, &ae, &md, &n_act, nullptr, nullptr,
+      GG_TRY((L.small_run<PushOp, false, T>(dout, PushOp{cur, msg}, q, &c_i, &nq, &ae, &md, &n_act, nullptr, nullptr,
                                             cur, msg, tr, stamp)));
       continue;
     }
     tr.add(sparse ? 0 : 1, ae, 0);
     int nx = c_i ^ 1;
-    if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[c_i], g->out.nz, q[c_i], &nq));
+    if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[c_i], dout.nz, q[c_i], &nq));
     GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
     GG_TRY(counters_reset(g));
     ActOut a;
     a.active_out = bm[nx];
     a.q_out = sparse ? q[nx] : nullptr;
     a.qlen = &ctr->qlen;
-    a.out_deg = g->out.deg;
+    a.out_deg = dout.deg;
     a.queue_nonzero_only = true;
     if (sparse) {
       if (ae > 0) {
         gather_by_queue<T><<<grid_for(nq, 256, g->num_sms), 256, 0, s>>>(q[c_i], nq, cur, msg);
         unsigned long long *P;
-        GG_TRY(L.scan_queue_degrees(q[c_i], nq, g->out.deg, &P));
+        GG_TRY(L.scan_queue_degrees(q[c_i], nq, dout.deg, &P));
         GG_TRY(tr.kbegin());
-        push_lb<PushOp><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[c_i], P, nq, ae, g->out, PushOp{cur, msg}, a,
+        push_lb<PushOp><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(q[c_i], P, nq, ae, dout, PushOp{cur, msg}, a,
                                                                    ctr);
         GG_TRY(tr.kend());
         L.launches += 2;
       }
     } else {
       GG_TRY(tr.kbegin());
-      GG_TRY(L.pull(g->in, PullOp{cur, nxt}, a, ctr));
+      PullOp op = pull;
+      op.cur = cur;
+      op.nxt = nxt;
+      GG_TRY(L.pull(din, op, a, ctr));
       GG_TRY(tr.kend());
       T *t = cur;
       cur = nxt;
@@ -167,6 +171,13 @@ static int relax_loop(gg_graph *g, T *state0, T *state1, uint32_t *q0, uint32_t 
   return GG_OK;
 }
 
+// out[v] = by_rank[rank_of[v]]
+__global__ void unrank_u32(const uint32_t *__restrict__ by_rank, const uint32_t *__restrict__ rank_of, uint32_t V,
+                           uint32_t *__restrict__ out) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    out[v] = by_rank[rank_of[v]];
+}
+
 static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   GG_CUDA(cudaSetDevice(g->device));
   const uint32_t V = g->V;
@@ -178,18 +189,39 @@ static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   GG_TRY(ws(g, WS_BM2, words, &bm[1]));
   GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
   GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
+  // On a symmetric graph the hot-source layout (vertices renumbered by
+  // descending degree, built once and shared with PageRank) packs the most
+  // gathered labels into few cache lines.  Labels stay vertex ids, so the
+  // minimum is the reference's; they map back to vertex order at the end.
+  if (g->symmetric && g->pr_layout) GG_TRY(pr_layout_build(g));
+  const bool ranked = g->symmetric && g->pr_layout && g->pr_ready;
+  const Dir &dout = ranked ? g->pr : g->out;
+  const Dir &din = ranked ? g->pr : g->in;
+  uint32_t *out = nullptr;
+  if (ranked) GG_TRY(ws(g, WS_S2, V, &out));
   Launch L(g);
   Trace tr(st, g);
   cudaStream_t s = g->stream;
   GG_TRY(timed_begin(g));
   // label[v] = v over active_in = all (cc.cpp:31-37)
-  iota_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(lab[0], V);
+  if (ranked)
+    GG_CUDA(cudaMemcpyAsync(lab[0], g->pr_id_of_rank, sizeof(uint32_t) * V, cudaMemcpyDeviceToDevice, s));
+  else
+    iota_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(lab[0], V);
   bitmap_fill<<<grid_for(words, 256, g->num_sms), 256, 0, s>>>(bm[0], words, V);
-  L.launches += 2;
+  L.launches += ranked ? 1 : 2;
   GG_CUDA(cudaGetLastError());
   uint32_t *res = nullptr;
-  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0, 0xffffffffu, false, g->nadj,
-                                               tr, L, &res)));
+  CcPull pull{};
+  pull.ids = ranked ? g->pr_id_of_rank : nullptr;
+  GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, dout, din, pull, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0,
+                                               0xffffffffu, false, g->nadj, tr, L, &res)));
+  if (ranked) {
+    unrank_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(res, g->pr_rank_of, V, out);
+    L.launches += 1;
+    GG_CUDA(cudaGetLastError());
+    res = out;
+  }
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
   if (label_host) GG_CUDA(cudaMemcpy(label_host, res, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost));
@@ -240,7 +272,8 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   Counters c;
   GG_TRY(counters_read(g, &c));
   float *res = nullptr;
-  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1, 1, c.maxdeg, true, c.edges,
+  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, g->out, g->in, SsspPull{}, dist[0], dist[1], q[0], q[1], bm[0], bm[1],
+                                                1, 1, c.maxdeg, true, c.edges,
                                                 tr, L, &res)));
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());

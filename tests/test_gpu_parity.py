@@ -375,6 +375,26 @@ def test_autotune_picks_and_caches(tmp_path):
 
 
 @pytest.mark.parametrize("name", ["rmat16", "grid128", "random_odd"])
+def test_cc_layouts_agree(name):
+    """CC on a symmetric graph runs on the hot-source layout by default (labels
+    stay vertex ids, mapped back to vertex order); the plain adjacency gives
+    the same labels and the same per-call trace, both equal to the oracle's."""
+    V, s, d, w, _ = case(name)
+    g = gg.Graph.from_edges(V, s, d, symmetric=True)
+    olabel, otrace = OracleGraph(V, s, d, symmetric=True).cc()
+    hot, st = g.cc()
+    g.set_pr_layout(False)
+    plain, st2 = g.cc()
+    assert np.array_equal(hot, olabel) and np.array_equal(plain, olabel)
+    assert st.rows() == otrace and st2.rows() == otrace
+    g.set_pr_layout(True)
+    ranks_hot = g.pagerank(5)[0]
+    again, _ = g.cc()
+    assert np.array_equal(again, olabel)
+    assert rel_l1(ranks_hot, OracleGraph(V, s, d, symmetric=True).pagerank(5)[0]) < PR_TOL
+
+
+@pytest.mark.parametrize("name", ["rmat16", "grid128", "random_odd"])
 def test_pagerank_layouts_agree(name):
     """The hot-source layout (default) and the plain incoming adjacency give
     the same ranks up to summation order, both within tolerance of the

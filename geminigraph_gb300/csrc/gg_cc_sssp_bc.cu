@@ -259,6 +259,24 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   GG_TRY(ws(g, WS_BM2, words, &bm[1]));
   GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
   GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
+  // Hot-source layout (as PageRank's and CC's): both directions renumbered
+  // by descending out-degree, weights carried along.  Every candidate
+  // distance d[u] + w is the same sum, and a minimum does not depend on
+  // order, so the distances are bit-identical; they map back to vertex order
+  // at the end.
+  if (g->pr_layout) {
+    GG_TRY(pr_layout_build(g));
+    if (!g->symmetric) GG_TRY(hot_out_build(g));
+  }
+  const bool ranked = g->pr_layout && g->pr_ready && (g->symmetric || g->pr_out_ready);
+  const Dir &dout = ranked ? (g->symmetric ? g->pr : g->pr_out) : g->out;
+  const Dir &din = ranked ? g->pr : g->in;
+  uint32_t start = root;
+  float *out = nullptr;
+  if (ranked) {
+    GG_CUDA(cudaMemcpy(&start, g->pr_rank_of + root, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    GG_TRY(ws(g, WS_S2, V, &out));
+  }
   Launch L(g);
   Trace tr(st, g);
   cudaStream_t s = g->stream;
@@ -266,15 +284,21 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   GG_CUDA(cudaMemsetAsync(bm[0], 0, words * 4, s));
   GG_TRY(counters_reset(g));
   fill_kernel<float><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(dist[0], V, 1e9f);
-  sssp_root<<<1, 1, 0, s>>>(dist[0], root, bm[0], q[0], g->out.deg, g->ws.ctr);
+  sssp_root<<<1, 1, 0, s>>>(dist[0], start, bm[0], q[0], dout.deg, g->ws.ctr);
   L.launches += 2;
   GG_CUDA(cudaGetLastError());
   Counters c;
   GG_TRY(counters_read(g, &c));
   float *res = nullptr;
-  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, g->out, g->in, SsspPull{}, dist[0], dist[1], q[0], q[1], bm[0], bm[1],
-                                                1, 1, c.maxdeg, true, c.edges,
-                                                tr, L, &res)));
+  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dout, din, SsspPull{}, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1,
+                                                1, c.maxdeg, true, c.edges, tr, L, &res)));
+  if (ranked) {
+    unrank_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>((const uint32_t *)res, g->pr_rank_of, V,
+                                                            (uint32_t *)out);
+    L.launches += 1;
+    GG_CUDA(cudaGetLastError());
+    res = out;
+  }
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
   if (dist_host) GG_CUDA(cudaMemcpy(dist_host, res, sizeof(float) * V, cudaMemcpyDeviceToHost));

@@ -122,6 +122,7 @@ constexpr size_t STAGE_BYTES_HOST = 64 * 1024;
 class LanePool;
 void pools_destroy(gg_graph *g);
 int pr_layout_build(gg_graph *g);
+int hot_out_build(gg_graph *g);
 void pr_layout_free(gg_graph *g);
 
 }  // namespace gg
@@ -158,6 +159,10 @@ struct gg_graph {
   uint32_t *pr_id_of_rank = nullptr;  // V: vertex with new number r
   uint32_t *pr_od = nullptr;          // V: out-degree in the new numbering
   bool pr_ready = false;
+  // the outgoing adjacency in the same numbering (directed graphs; built on
+  // demand by SSSP, whose push steps walk out-lists)
+  gg::Dir pr_out;
+  bool pr_out_ready = false;
   int pr_layout = 1;                  // 0: PageRank pulls the plain incoming adjacency
   // batched SSSP bucket width (0: plain Bellman-Ford rounds) and the least
   // edge weight (bucketing needs none negative), found on first use

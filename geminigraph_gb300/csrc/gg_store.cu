@@ -511,6 +511,12 @@ int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk, uint32_t vec) {
     g->pr.chunk = chunk;
     GG_TRY(build_bins(g, &g->pr));
   }
+  if (g->pr_out_ready) {
+    free_bins(g, &g->pr_out);
+    g->pr_out.light = light;
+    g->pr_out.chunk = chunk;
+    GG_TRY(build_bins(g, &g->pr_out));
+  }
   return GG_OK;
 }
 
@@ -659,24 +665,78 @@ __global__ void rank_edge_keys_big(Dir d, int bits, const uint32_t *__restrict__
   }
 }
 
+// Frees a renumbered direction and its device bytes.
+static void free_hot_dir(gg_graph *g, Dir *d) {
+  const size_t V = g->V;
+  free_bins(g, d);
+  const size_t npad = (g->nadj + 64) / 64 * 64;
+  g->graph_bytes -= sizeof(uint64_t) * (V + 1) + sizeof(uint32_t) * (npad + V + 1) +
+                    sizeof(uint32_t) * bitmap_words32(g->V) + (d->w ? sizeof(float) * (g->nadj ? g->nadj : 1) : 0);
+  if (d->off) cudaFree(d->off);
+  if (d->nbr) cudaFree(d->nbr);
+  if (d->w) cudaFree(d->w);
+  if (d->deg) cudaFree(d->deg);
+  if (d->nz) cudaFree(d->nz);
+  *d = Dir();
+}
+
 void pr_layout_free(gg_graph *g) {
   if (!g->pr_ready) return;
   cudaStreamSynchronize(g->stream);
   const size_t V = g->V;
   g->graph_bytes -= sizeof(uint32_t) * 3 * V;
-  free_bins(g, &g->pr);
-  const size_t npad = (g->nadj + 64) / 64 * 64;
-  g->graph_bytes -= sizeof(uint64_t) * (V + 1) + sizeof(uint32_t) * (npad + V + 1) + sizeof(uint32_t) * bitmap_words32(g->V);
-  if (g->pr.off) cudaFree(g->pr.off);
-  if (g->pr.nbr) cudaFree(g->pr.nbr);
-  if (g->pr.deg) cudaFree(g->pr.deg);
-  if (g->pr.nz) cudaFree(g->pr.nz);
+  free_hot_dir(g, &g->pr);
+  if (g->pr_out_ready) free_hot_dir(g, &g->pr_out);
+  g->pr_out_ready = false;
   cudaFree(g->pr_rank_of);
   cudaFree(g->pr_id_of_rank);
   cudaFree(g->pr_od);
-  g->pr = Dir();
   g->pr_rank_of = g->pr_id_of_rank = g->pr_od = nullptr;
   g->pr_ready = false;
+}
+
+// src renumbered: list of rank r = the list of vertex id_of_rank[r], its
+// entries' neighbour ranks sorted ascending (weights carried along), built by
+// the load's radix sort.
+static int hot_dir(gg_graph *g, const Dir &src, Dir *dst, bool weights) {
+  const uint32_t V = g->V;
+  const size_t n = g->nadj;
+  const int bits = bits_for(V);
+  DevScratch tmp;
+  uint64_t *k0 = nullptr, *k1 = nullptr;
+  uint32_t *v0 = nullptr, *v1 = nullptr;
+  GG_TRY(tmp.get(&k0, n));
+  GG_TRY(tmp.get(&k1, n));
+  if (weights) {
+    GG_TRY(tmp.get(&v0, n));
+    GG_TRY(tmp.get(&v1, n));
+    if (n) GG_CUDA(cudaMemcpyAsync(v0, src.w, sizeof(float) * n, cudaMemcpyDefault, g->stream));
+  }
+  rank_edge_keys_light<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(src, V, bits, g->pr_rank_of, k0);
+  if (src.nbigchunks)
+    rank_edge_keys_big<<<grid_for((size_t)src.nbigchunks * 32, 256, g->num_sms, 16), 256, 0, g->stream>>>(
+        src, bits, g->pr_rank_of, k0);
+  GG_CUDA(cudaGetLastError());
+  *dst = Dir();
+  dst->light = src.light;
+  dst->chunk = src.chunk;
+  dst->vec = src.vec;
+  GG_TRY(build_dir(g, k0, v0, k1, v1, n, bits, dst, weights, false));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  return GG_OK;
+}
+
+int hot_out_build(gg_graph *g) {
+  if (g->pr_out_ready) return GG_OK;
+  GG_TRY(pr_layout_build(g));
+  GG_CUDA(cudaSetDevice(g->device));
+  const int s = hot_dir(g, g->out, &g->pr_out, g->weighted != 0);
+  if (s != GG_OK) {
+    free_hot_dir(g, &g->pr_out);
+    return s;
+  }
+  g->pr_out_ready = true;
+  return GG_OK;
 }
 
 int pr_layout_build(gg_graph *g) {
@@ -688,7 +748,7 @@ int pr_layout_build(gg_graph *g) {
   int dbits = 1;
   while (dbits < 32 && (1ull << dbits) <= n) dbits++;
   const uint32_t dmax = dbits >= 32 ? 0xFFFFFFFFu : (uint32_t)((1ull << dbits) - 1);
-  const size_t nk = n > V ? n : V;
+  const size_t nk = V;  // degree keys of the ranking sort
   uint64_t *k0 = nullptr, *k1 = nullptr;
   GG_CUDA(cudaMalloc(&g->pr_rank_of, sizeof(uint32_t) * V));
   GG_CUDA(cudaMalloc(&g->pr_id_of_rank, sizeof(uint32_t) * V));
@@ -707,24 +767,18 @@ int pr_layout_build(gg_graph *g) {
   if (status == GG_OK) {
     rank_tables<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(ks, V, bits, g->out.deg,
                                                                         g->pr_id_of_rank, g->pr_rank_of, g->pr_od);
-    const Dir &in = g->in;
-    rank_edge_keys_light<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(in, V, bits, g->pr_rank_of, k0);
-    if (in.nbigchunks)
-      rank_edge_keys_big<<<grid_for((size_t)in.nbigchunks * 32, 256, g->num_sms, 16), 256, 0, g->stream>>>(
-          in, bits, g->pr_rank_of, k0);
     e = cudaGetLastError();
     if (e != cudaSuccess) status = cuda_status(e, "PageRank layout");
-  }
-  if (status == GG_OK) {
-    g->pr = Dir();
-    g->pr.light = g->in.light;
-    g->pr.chunk = g->in.chunk;
-    g->pr.vec = g->in.vec;
-    status = build_dir(g, k0, nullptr, k1, nullptr, n, bits, &g->pr, false);
   }
   cudaStreamSynchronize(g->stream);
   if (k0) cudaFree(k0);
   if (k1) cudaFree(k1);
+  // the incoming adjacency renumbered, with its weights when the graph has
+  // them (SSSP's pulls gather them)
+  if (status == GG_OK) {
+    status = hot_dir(g, g->in, &g->pr, g->weighted != 0);
+    if (status != GG_OK) free_hot_dir(g, &g->pr);
+  }
   if (status != GG_OK) {
     cudaFree(g->pr_rank_of);
     cudaFree(g->pr_id_of_rank);

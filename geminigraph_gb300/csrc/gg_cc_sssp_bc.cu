@@ -172,8 +172,9 @@ static int relax_loop(gg_graph *g, const Dir &dout, const Dir &din, const PullOp
 }
 
 // out[v] = by_rank[rank_of[v]]
-__global__ void unrank_u32(const uint32_t *__restrict__ by_rank, const uint32_t *__restrict__ rank_of, uint32_t V,
-                           uint32_t *__restrict__ out) {
+template <typename T>
+__global__ void unrank(const T *__restrict__ by_rank, const uint32_t *__restrict__ rank_of, uint32_t V,
+                       T *__restrict__ out) {
   for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
     out[v] = by_rank[rank_of[v]];
 }
@@ -217,7 +218,7 @@ static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, dout, din, pull, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0,
                                                0xffffffffu, false, g->nadj, tr, L, &res)));
   if (ranked) {
-    unrank_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(res, g->pr_rank_of, V, out);
+    unrank<uint32_t><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(res, g->pr_rank_of, V, out);
     L.launches += 1;
     GG_CUDA(cudaGetLastError());
     res = out;
@@ -293,8 +294,7 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dout, din, SsspPull{}, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1,
                                                 1, c.maxdeg, true, c.edges, tr, L, &res)));
   if (ranked) {
-    unrank_u32<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>((const uint32_t *)res, g->pr_rank_of, V,
-                                                            (uint32_t *)out);
+    unrank<float><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(res, g->pr_rank_of, V, out);
     L.launches += 1;
     GG_CUDA(cudaGetLastError());
     res = out;
@@ -424,6 +424,22 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
   GG_TRY(ws(g, WS_BM2, words, &bm[1]));
   GG_TRY(ws(g, WS_BM3, words, &lvbm));
   GG_TRY(ws(g, WS_QLEV, (size_t)V + 2, &qlev));
+  // Hot-source layout (as SSSP's): both directions renumbered; path counts
+  // are exact and dependencies change only in summation order.
+  if (g->pr_layout) {
+    GG_TRY(pr_layout_build(g));
+    if (!g->symmetric) GG_TRY(hot_out_build(g));
+  }
+  const bool ranked = g->pr_layout && g->pr_ready && (g->symmetric || g->pr_out_ready);
+  const Dir &dout = ranked ? (g->symmetric ? g->pr : g->pr_out) : g->out;
+  const Dir &din = ranked ? g->pr : g->in;
+  uint32_t start = root;
+  double *dep_out = dep, *np_out = np;
+  if (ranked) {
+    GG_CUDA(cudaMemcpy(&start, g->pr_rank_of + root, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    GG_TRY(ws(g, WS_S0, V, &dep_out));
+    GG_TRY(ws(g, WS_S1, V, &np_out));
+  }
   Launch L(g);
   Trace tr(st, g);
   cudaStream_t s = g->stream;
@@ -433,7 +449,7 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
   GG_CUDA(cudaMemsetAsync(bm[0], 0, words * 4, s));
   GG_TRY(counters_reset(g));
   fill_kernel<double><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(np, V, 0.0);
-  bc_root<<<1, 1, 0, s>>>(np, root, visited, bm[0], qlev, g->out.deg, g->in.deg, ctr);
+  bc_root<<<1, 1, 0, s>>>(np, start, visited, bm[0], qlev, dout.deg, din.deg, ctr);
   L.launches += 2;
   GG_CUDA(cudaGetLastError());
   Counters c;
@@ -454,23 +470,23 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
     a.active_out = bm[nx];
     a.q_out = qlev + lev_off.back();
     a.qlen = &ctr->qlen;
-    a.out_deg = g->out.deg;
-    a.in_deg = g->in.deg;
+    a.out_deg = dout.deg;
+    a.in_deg = din.deg;
     const uint32_t *qin = qlev + lev_off[L_];
     a.q_out = sparse ? qlev + lev_off.back() : nullptr;
     if (sparse) {
       if (ae > 0) {
         unsigned long long *P;
-        GG_TRY(L.scan_queue_degrees(qin, n, g->out.deg, &P));
+        GG_TRY(L.scan_queue_degrees(qin, n, dout.deg, &P));
         GG_TRY(tr.kbegin());
-        push_lb<BcFwdPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(qin, P, n, ae, g->out, BcFwdPush{np, visited},
+        push_lb<BcFwdPush><<<L.push_grid(ae), PUSH_THREADS, 0, s>>>(qin, P, n, ae, dout, BcFwdPush{np, visited},
                                                                       a, ctr);
         GG_TRY(tr.kend());
         L.launches += 1;
       }
     } else {
       GG_TRY(tr.kbegin());
-      GG_TRY(L.pull(g->in, BcFwdPull{np, bm[cur], visited}, a, ctr));
+      GG_TRY(L.pull(din, BcFwdPull{np, bm[cur], visited}, a, ctr));
       GG_TRY(tr.kend());
     }
     GG_CUDA(cudaGetLastError());
@@ -495,7 +511,7 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
   GG_CUDA(cudaMemsetAsync(visited, 0, words * 4, s));
   L.launches += 1;
   // backward on the transposed graph: push over the CSC, pull over the CSR
-  const Dir &tout = g->in, &tin = g->out;
+  const Dir &tout = din, &tin = dout;
   for (int lev = top; lev >= 1; lev--) {
     uint32_t ln = (uint32_t)(lev_off[lev + 1] - lev_off[lev]);
     const uint32_t *ql = qlev + lev_off[lev];
@@ -528,13 +544,18 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
   }
   bc_final<<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(dep, np, V);
   L.launches += 1;
+  if (ranked) {
+    unrank<double><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(dep, g->pr_rank_of, V, dep_out);
+    unrank<double><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(np, g->pr_rank_of, V, np_out);
+    L.launches += 2;
+  }
   GG_CUDA(cudaGetLastError());
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
-  if (dep_host) GG_CUDA(cudaMemcpy(dep_host, dep, sizeof(double) * V, cudaMemcpyDeviceToHost));
-  if (inv_host) GG_CUDA(cudaMemcpy(inv_host, np, sizeof(double) * V, cudaMemcpyDeviceToHost));
-  g->result[0] = dep;
-  g->result[1] = np;
+  if (dep_host) GG_CUDA(cudaMemcpy(dep_host, dep_out, sizeof(double) * V, cudaMemcpyDeviceToHost));
+  if (inv_host) GG_CUDA(cudaMemcpy(inv_host, np_out, sizeof(double) * V, cudaMemcpyDeviceToHost));
+  g->result[0] = dep_out;
+  g->result[1] = np_out;
   return GG_OK;
 }
 

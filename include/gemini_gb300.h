@@ -357,10 +357,10 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
  * ranks differ from the plain layout's in the last bits only.  hot_sources =
  * 0 frees the copy and pulls the plain incoming adjacency.  The copy is
  * dropped by gg_graph_transpose and counted in device_bytes.  gg_cc on a
- * symmetric graph uses the same copy, and gg_sssp uses it together with the
- * outgoing adjacency in the same numbering (built on its first call on a
- * directed graph), weights carried along: labels and distances are identical
- * either way. */
+ * symmetric graph uses the same copy, and gg_sssp and gg_bc use it together
+ * with the outgoing adjacency in the same numbering (built on their first
+ * call on a directed graph), weights carried along: labels and distances are
+ * identical either way, BC dependencies equal up to summation order. */
 int gg_graph_set_pr_layout(gg_graph *g, int hot_sources);
 
 /* ---- engine primitives ---- */

@@ -530,7 +530,7 @@ class Server:
 
 
 def pick_roots(out_degree, count, seed):
-    """Seeded uniform draws of vertices with out-degree > 0 (BASELINE's
+    """Seeded uniform draws of vertices with out-degree > 0 (the benchmark's
     "non-isolated" roots)."""
     rng = np.random.default_rng(seed)
     cand = np.nonzero(np.asarray(out_degree) > 0)[0]

@@ -60,3 +60,16 @@ def test_reference_arm_under_torchrun_prints_once():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] in ("reference", "port")
+
+
+def test_reference_arm_build_workload_is_unavailable():
+    """The reference's loader reports no load time, so its arm for the build
+    workload prints the one-line unavailable record and exits 0."""
+    cmd = [sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--workload", "build",
+           "--steps", "1", "--warmup", "0"]
+    p = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=REPO)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and "unavailable" in d

@@ -24,6 +24,16 @@ engine) / time.
 same sample, printed with impl=reference.  Multi-GPU (torchrun): replicas --
 each rank runs its own BFSes on its own GPU; value = all ranks' edges / the
 slowest rank's time.
+
+Other workloads (--workload): cc, pagerank, pagerank_f64, sssp, bc, bfs_grid
+(GTEPS as above); bfs_batched, sssp_batched, bc_batched (queries/s of
+64-root batches beside the same roots run one at a time); serve (continuous
+batching over four resident graphs, p50/p99 latency beside a plain FIFO
+replay; --mix adds plain vs full-batch costs per graph and kind); build (the
+partitioned graph build from records in pinned host memory under
+--build-budget-gb, Medges/s, beside the in-core build).  --adjacency host
+keeps the neighbour arrays in mapped host memory (read over NVLink-C2C) and
+adds the link rate to the roofline; --bins default skips the autotuner.
 """
 import argparse
 import json

@@ -448,15 +448,24 @@ int build_plan(gg_graph *g, uint64_t E, bool rec_on_device, const gg_build_optio
   *gcap = 0;
   if (!*partitioned) return GG_OK;
   if (force) return GG_OK;
-  // (range, tile) counts (room for 64 ranges) + the offsets scan; then a
-  // group buffer of G entries (key + value) and one range's sort buffer and
-  // digit counts, ranges of at most G/4 entries
+  // (range, tile) counts and their scan (8 B per tile and range) + the
+  // offsets scan; then a group buffer of G entries (key + value) and one
+  // range's sort buffer and digit counts, ranges of at most G/4 entries.
+  // Greedy ranges of at most cap entries number at most 2n/cap + 1, so the
+  // count table is sized for that many (at least 64), refined until it fits.
   const uint64_t tiles = (n + OC_TILE - 1) / OC_TILE;
-  const uint64_t fixed = (uint64_t)g->V * 8 + tiles * 8 * 64 + (64ull << 20);
   const uint64_t kv = 8 + (g->weighted ? 4 : 0);
-  const uint64_t avail = budget > fixed ? budget - fixed : 0;
-  *gcap = avail * 4 / (4 * kv + kv + 1);
-  *cap = *gcap / 4;
+  uint64_t ranges = 64;
+  for (int it = 0; it < 4; it++) {
+    const uint64_t fixed = (uint64_t)g->V * 8 + tiles * 8 * ranges + (64ull << 20);
+    const uint64_t avail = budget > fixed ? budget - fixed : 0;
+    *gcap = avail * 4 / (4 * kv + kv + 1);
+    *cap = *gcap / 4;
+    if (*cap == 0) break;
+    const uint64_t need = std::min<uint64_t>(2 * n / *cap + 1, OC_MAX_PARTS);
+    if (need <= ranges) break;
+    ranges = need;
+  }
   if (*cap < (1ull << 16) && *cap < n) {
     set_error("build needs %llu device bytes beyond the graph; %llu available", (unsigned long long)in_core,
               (unsigned long long)budget);

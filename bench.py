@@ -279,97 +279,170 @@ def step_args(gg, g, workload, count):
         return [None] * count
     if workload == "bfs_grid":
         return [0] * count
-    return gg.pick_roots(g.out_degree(), count, seed=SEED + 1000)
+    return gg.pick_roots(g.out_degree(), count, seed=root_seed(workload))
 
 
 # ----------------------------------------------------------------- CPU side
+# Workloads whose reference run is timed on the benchmark's own graph and
+# roots: the reference's BFS driver reports each run's traversed edges itself
+# (teps_edges, read from its parent array), so no oracle trace is needed.
+FULL_SCALE_REFERENCE = ("bfs",)
+
+
 def ref_sample_scale(workload):
-    return {"bfs": 22, "cc": 21, "pagerank": 20, "pagerank_f64": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024, "bfs_batched": 22,
-            "sssp_batched": 21, "bc_batched": 21, "serve": 22}[workload]
+    """Graph the reference is timed on: the workload's own scale where the
+    reference reports its TEPS numerator, else a bounded sample whose
+    numerator the oracle's per-call trace gives."""
+    if workload in FULL_SCALE_REFERENCE:
+        return WORKLOADS[workload]["scale"]
+    return {"cc": 21, "pagerank": 20, "pagerank_f64": 20, "sssp": 21, "bc": 21, "bfs_grid": 1024,
+            "bfs_batched": 22, "sssp_batched": 21, "bc_batched": 21, "serve": 22}[workload]
 
 
-def cpu_reference(gg, workload, nsteps, warmup):
-    """Times the reference's own compute() (oracle/_ref/bin/ref_<app>) on a
-    bounded sample of the workload; falls back to the oracle port."""
-    from oracle.oracle import OracleGraph
+def root_seed(workload):
+    """Seed of the workload's root sequence; the GPU arm draws the same one."""
+    return SEED + 1000 if workload in ("bfs", "sssp", "bc") else SEED + 2000
+
+
+def scratch_dir(nbytes):
+    """RAM-backed /dev/shm when it has room for the edge file, else the default temp dir."""
+    try:
+        st = os.statvfs("/dev/shm")
+        if st.f_bavail * st.f_frsize > 2 * nbytes:
+            return "/dev/shm"
+    except OSError:
+        pass
+    return None
+
+
+def cpu_reference(workload, nsteps, warmup, first_root=0):
+    """Times the reference's own compute() (oracle/_ref/bin/ref_<app>, the
+    reference's sources built on this host) with every host core; falls back
+    to the oracle port.  The edge file and the roots come from the oracle's
+    restatement of the benchmark generator and root rule, so this leg loads no
+    product code.  For FULL_SCALE_REFERENCE workloads the graph is the
+    benchmark's own and the roots are the GPU arm's roots first_root,
+    first_root + 1, ... (warm-up roots first)."""
+    from oracle import oracle
     w = WORKLOADS[workload]
     s = ref_sample_scale(workload)
-    if w["kind"] == "rmat":
-        V = 1 << s
-        rec = gg.generate_records(gg.RMAT, s, w["ef"], SEED, weighted=w["weighted"])
-        sample = f"R-MAT scale {s}, edge factor {w['ef']}, seed {SEED}"
-    else:
-        V = s * s
-        rec = gg.generate_records(gg.GRID, s, 0, SEED, weighted=w["weighted"])
-        sample = f"{s} x {s} grid"
-    unit = 12 if w["weighted"] else 8
-    words = rec.view(np.uint32).reshape(-1, unit // 4)
-    src, dst = words[:, 0].copy(), words[:, 1].copy()
-    wts = words[:, 2].view(np.float32).copy() if w["weighted"] else None
-    n = warmup + nsteps
-    if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched", "bc_batched", "serve"):
-        args = gg.pick_roots(np.bincount(src, minlength=V), n, seed=SEED + 2000)
-    elif workload == "bfs_grid":
-        args = [0] * n
-    elif workload in ("pagerank", "pagerank_f64"):
-        args = [20] * n
-    else:
-        args = [0] * n
-    # TEPS numerators from the oracle's trace (the same quantity the reference counts)
-    og = OracleGraph(V, src, dst, wts, symmetric=w["symmetric"])
-    numer = []
-    for a in args:
-        if workload in ("bfs", "bfs_grid", "bfs_batched", "serve"):
-            tr = og.bfs(a)[1]
-        elif workload in ("sssp", "sssp_batched"):
-            tr = og.sssp(a)[1]
-        elif workload in ("bc", "bc_batched"):
-            tr = og.bc(a)[2]
-        elif workload in ("pagerank", "pagerank_f64"):
-            tr = og.pagerank(a)[2]
-        else:
-            tr = og.cc()[1]
-        numer.append(sum(r[1] for r in tr))
-    exe = os.path.join(REPO, "oracle", "_ref", "bin", "ref_" + REF_APP[workload])
     cores = os.cpu_count() or 1
-    if os.path.exists(exe):
-        fd, path = tempfile.mkstemp(suffix=".bin")
-        with os.fdopen(fd, "wb") as f:
-            f.write(rec.tobytes())
-        env = dict(os.environ, OMP_NUM_THREADS=str(cores), GG_REF_THREADS=str(cores))
-        try:
+    n = warmup + nsteps
+    kind = oracle.RMAT if w["kind"] == "rmat" else oracle.GRID
+    V = (1 << s) if kind == oracle.RMAT else s * s
+    unit = 12 if w["weighted"] else 8
+    nrec = oracle.record_count(kind, s, w["ef"])
+    sample = (f"R-MAT scale {s}, edge factor {w['ef']}, seed {SEED}" if kind == oracle.RMAT else f"{s} x {s} grid")
+    if s == w["scale"]:
+        sample += " (the benchmark's graph)"
+    fd, path = tempfile.mkstemp(suffix=".bin", dir=scratch_dir(nrec * unit))
+    os.close(fd)
+    try:
+        t0 = time.perf_counter()
+        V, nrec, deg = oracle.write_records_file(path, kind, s, w["ef"], SEED, weighted=w["weighted"],
+                                                 threads=cores)
+        gen_s = time.perf_counter() - t0
+        if workload in ("bfs", "sssp", "bc", "bfs_batched", "sssp_batched", "bc_batched", "serve"):
+            args = oracle.pick_roots(deg, first_root + n, seed=root_seed(workload))[first_root:]
+            if s == w["scale"]:
+                sample += f"; roots {first_root}..{first_root + n - 1} of the benchmark's root sequence"
+        elif workload == "bfs_grid":
+            args = [0] * n
+        elif workload in ("pagerank", "pagerank_f64"):
+            args = [20] * n
+        else:
+            args = [0] * n
+        numer = None
+        if workload not in FULL_SCALE_REFERENCE:
+            # TEPS numerators from the oracle's trace (the quantity the reference counts)
+            rec = np.fromfile(path, dtype=np.uint32).reshape(-1, unit // 4)
+            og = oracle.OracleGraph(V, rec[:, 0].copy(), rec[:, 1].copy(),
+                                    rec[:, 2].copy().view(np.float32) if w["weighted"] else None,
+                                    symmetric=w["symmetric"])
+            del rec
+            numer = [sum(r[1] for r in oracle_trace(og, workload, a)) for a in args]
+        exe = os.path.join(REPO, "oracle", "_ref", "bin", "ref_" + REF_APP[workload])
+        if os.path.exists(exe):
+            env = dict(os.environ, OMP_NUM_THREADS=str(cores), GG_REF_THREADS=str(cores))
             p = subprocess.run([exe, path, str(V)] + [str(a) for a in args], capture_output=True, text=True,
-                               env=env, timeout=900)
-        finally:
-            os.unlink(path)
-        times = [float(x) for x in re.findall(r"exec_time=([0-9.]+)", p.stdout)]
-        if p.returncode == 0 and len(times) == n:
-            t = times[warmup:]
-            e = numer[warmup:]
-            return dict(value=sum(e) / sum(t) / 1e9, unit="GTEPS", cores=cores, kind="reference",
-                        sample=f"{sample}; {nsteps} timed runs after {warmup} warm-up; reference compute() "
-                               f"exec_time, {cores} OpenMP threads", times=t, edges=e)
-        log("reference driver failed:", p.returncode, p.stderr[-500:])
-    # oracle port: serial C restatement
+                               env=env, timeout=1500)
+            times = [float(x) for x in re.findall(r"exec_time=([0-9.]+)", p.stdout)]
+            counted = [int(x) for x in re.findall(r"teps_edges=([0-9]+)", p.stdout)]
+            load = re.findall(r"load_time=([0-9.]+)", p.stdout)
+            if numer is None and len(counted) == n:
+                numer = counted
+            if p.returncode == 0 and len(times) == n and numer is not None:
+                t = times[warmup:]
+                e = numer[warmup:]
+                return dict(value=sum(e) / sum(t) / 1e9, unit="GTEPS", cores=cores, kind="reference",
+                            sample=f"{sample}; {nsteps} timed runs after {warmup} warm-up; reference compute() "
+                                   f"exec_time, {cores} OpenMP threads", times=t, edges=e,
+                            load_s=float(load[0]) if load else None, generate_s=round(gen_s, 1))
+            log("reference driver failed:", p.returncode, p.stderr[-500:])
+        if numer is None:
+            raise RuntimeError("the reference driver did not run and the oracle port has no numerators")
+        # oracle port: serial C restatement
+        rec = np.fromfile(path, dtype=np.uint32).reshape(-1, unit // 4)
+        og = oracle.OracleGraph(V, rec[:, 0].copy(), rec[:, 1].copy(),
+                                rec[:, 2].copy().view(np.float32) if w["weighted"] else None,
+                                symmetric=w["symmetric"])
+        del rec
+    finally:
+        os.unlink(path)
     t, e = [], []
     for i, a in enumerate(args):
         t0 = time.perf_counter()
-        if workload in ("bfs", "bfs_grid", "bfs_batched", "serve"):
-            og.bfs(a)
-        elif workload in ("sssp", "sssp_batched"):
-            og.sssp(a)
-        elif workload in ("bc", "bc_batched"):
-            og.bc(a)
-        elif workload in ("pagerank", "pagerank_f64"):
-            og.pagerank(a)
-        else:
-            og.cc()
+        oracle_trace(og, workload, a)
         if i >= warmup:
             t.append(time.perf_counter() - t0)
             e.append(numer[i])
     return dict(value=sum(e) / sum(t) / 1e9, unit="GTEPS", cores=1, kind="port",
                 sample=f"{sample}; {nsteps} timed runs after {warmup} warm-up; oracle port, 1 thread",
                 times=t, edges=e)
+
+
+def _boot_id():
+    try:
+        return open("/proc/sys/kernel/random/boot_id").read().strip()
+    except OSError:
+        return None
+
+
+def _reference_cache_path(workload):
+    return os.path.join(tempfile.gettempdir(), f"gg_reference_{workload}_s{ref_sample_scale(workload)}.json")
+
+
+def save_reference_result(workload, r):
+    """Keeps the reference arm's result for this host's later GPU run (the
+    reference's own load of an R-MAT 26 file takes minutes)."""
+    try:
+        with open(_reference_cache_path(workload), "w") as f:
+            json.dump(dict(r, boot_id=_boot_id(), when=time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())), f)
+    except OSError:
+        pass
+
+
+def cached_reference_result(workload):
+    """The reference arm's result from this boot of this host, if any."""
+    try:
+        r = json.load(open(_reference_cache_path(workload)))
+    except (OSError, ValueError):
+        return None
+    if r.get("boot_id") != _boot_id() or r.get("boot_id") is None or r.get("kind") != "reference":
+        return None
+    return r
+
+
+def oracle_trace(og, workload, a):
+    if workload in ("bfs", "bfs_grid", "bfs_batched", "serve"):
+        return og.bfs(a)[1]
+    if workload in ("sssp", "sssp_batched"):
+        return og.sssp(a)[1]
+    if workload in ("bc", "bc_batched"):
+        return og.bc(a)[2]
+    if workload in ("pagerank", "pagerank_f64"):
+        return og.pagerank(a)[2]
+    return og.cc()[1]
 
 
 # ----------------------------------------------------------------- arms
@@ -380,9 +453,9 @@ def reference_arm(args, dist):
         print(json.dumps({"impl": "reference", "unavailable": "the reference's loader reports no load time of its "
                           "own (its toolkits time compute() only)"}), flush=True)
         return 0
-    import geminigraph_gb300 as gg
     w = WORKLOADS[args.workload]
-    r = cpu_reference(gg, args.workload, args.steps, args.warmup)
+    r = cpu_reference(args.workload, args.steps, args.warmup)
+    save_reference_result(args.workload, r)
     if args.workload.endswith("_batched") or args.workload == "serve":
         # the reference has no batching: its queries/s is one root at a time
         r["value"], r["unit"] = len(r["times"]) / sum(r["times"]), "queries/s"
@@ -544,9 +617,15 @@ def gpu_arm(args, dist):
                                     "peak_source": "measured pinned host->device copy (torch, CUDA events)"}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         try:
-            r = cpu_reference(gg, args.workload, 5, 1)
+            r = cached_reference_result(args.workload)
+            if r is not None:
+                r["sample"] += f"; measured by this host's reference arm (bench.py --impl reference) at {r['when']}"
+            else:
+                # bounded: one warm-up and three timed roots, the first of the sequence timed above
+                r = cpu_reference(args.workload, 3, 1, first_root=max(args.warmup - 1, 0))
             line["cpu_baseline"] = {k: (round(r[k], 4) if k == "value" else r[k])
                                     for k in ("value", "unit", "cores", "kind", "sample")}
+            line["cpu_baseline"]["reference_load_s"] = r.get("load_s")
         except Exception as e:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
     if dist.rank == 0:

@@ -3,7 +3,8 @@
 # reference's own sources, for use as test infrastructure and as the CPU
 # baseline.  Outputs go only to oracle/_ref/ (git-ignored).
 #
-# Step 1 (only where the reference checkout exists): stage the reference's
+# Usage: build_ref.sh [<reference checkout>]  (or GG_REFERENCE_DIR=<dir>).
+# Step 1 (only where a reference checkout is given): stage the reference's
 #   core/*.hpp and toolkits/*.cpp into oracle/_ref/src/, applying two patches
 #   to the staged copy of core/graph.hpp:
 #     a. core/graph.hpp:240  `T * dealloc_vertex_array` -> `void ...`.  The
@@ -17,12 +18,12 @@
 #   (-O3 -std=c++11 -fopenmp -march=native), into oracle/_ref/bin/.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${GG_REFERENCE_DIR:-/root/reference}"
+REF="${1:-${GG_REFERENCE_DIR:-}}"
 OUT="$HERE/_ref"
 SRC="$OUT/src"
 BIN="$OUT/bin"
 
-if [ -f "$REF/core/graph.hpp" ]; then
+if [ -n "$REF" ] && [ -f "$REF/core/graph.hpp" ]; then
   mkdir -p "$SRC/core" "$SRC/toolkits"
   cp "$REF"/core/*.hpp "$SRC/core/"
   cp "$REF"/toolkits/*.cpp "$SRC/toolkits/"
@@ -53,7 +54,8 @@ done
 # drivers: the same toolkits' compute() over several roots on one loaded graph
 for app in bfs cc pagerank sssp bc; do
   APP=$(echo "$app" | tr a-z A-Z)
-  if [ "$BIN/ref_$app" -nt "$HERE/ref_driver.cpp" ] && [ "$BIN/ref_$app" -nt "$SRC/core/graph.hpp" ]; then
+  if [ "$BIN/ref_$app" -nt "$HERE/ref_driver.cpp" ] && [ "$BIN/ref_$app" -nt "$SRC/core/graph.hpp" ] &&
+     [ "$BIN/ref_$app" -nt "$HERE/shim/numa.h" ] && [ "$BIN/ref_$app" -nt "$HERE/shim/mpi.h" ]; then
     continue
   fi
   "$CXX" -O3 -std=c++11 -g -fopenmp -march=native -w -DGG_APP_$APP \

@@ -579,3 +579,120 @@ int orc_bc(orc_graph *g, uint32_t root, double *dep, double *inv, orc_trace *tr)
   free(msg);
   return calls;
 }
+
+/* ---- seeded synthetic edge lists (inputs of the CPU baseline and tests) ----
+ *
+ * Restates the benchmark's input generator so that the reference can be fed
+ * the same bytes without the product library.  Counter-based: record e
+ * depends only on (seed, e).
+ *   key          = mix64(seed ^ 0x5851F42D4C957F2D)
+ *   draw64(e, j) = mix64(key + (e * 64 + j) * 0x9E3779B97F4A7C15)  (mod 2^64)
+ * mix64 is the SplitMix64 finaliser (Steele, Lea, Flood, OOPSLA 2014).
+ * R-MAT (Chakrabarti, Zhan, Faloutsos, SDM 2004), a=.57 b=.19 c=.19 d=.05:
+ * level l (most significant bit first) takes 32 bits of draw64(e, l/2) (low
+ * half for even l, high for odd l); u >= floor(.76*2^32) sets the source bit,
+ * floor(.57*2^32) <= u < floor(.76*2^32) or u >= floor(.95*2^32) the
+ * destination bit.  Weight: (low32(draw64(e, 16)) >> 8) * 2^-24.
+ * Grid n x n: per vertex v = r*n+c in row-major order the records (v,v+1),
+ * (v+1,v) when c+1 < n, then (v,v+n), (v+n,v) when r+1 < n.
+ * Records are the reference's packed EdgeUnit (core/type.hpp:27-41): two
+ * uint32 words, plus the float32 weight as a third word when weighted. */
+static uint64_t orc_mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static uint64_t orc_draw(uint64_t key, uint64_t e, uint32_t j) {
+  return orc_mix64(key + (e * 64u + j) * 0x9E3779B97F4A7C15ull);
+}
+
+static uint32_t orc_weight_bits(uint64_t key, uint64_t e) {
+  float w = (float)((uint32_t)orc_draw(key, e, 16) >> 8) * (1.0f / 16777216.0f);
+  uint32_t bits;
+  memcpy(&bits, &w, 4);
+  return bits;
+}
+
+/* Records [first, first + count) of R-MAT `scale` into out (2 or 3 words each). */
+void orc_rmat_records(uint32_t scale, uint64_t seed, int weighted, uint64_t first, uint64_t count,
+                      uint32_t *out) {
+  const uint32_t ta = 2448131358u, tab = 3264175144u, tabc = 4080218931u;
+  uint64_t key = orc_mix64(seed ^ 0x5851F42D4C957F2Dull);
+  int words = weighted ? 3 : 2;
+  for (uint64_t i = 0; i < count; i++) {
+    uint64_t e = first + i;
+    uint32_t s = 0, d = 0;
+    uint64_t draw = 0;
+    for (uint32_t l = 0; l < scale; l++) {
+      if ((l & 1u) == 0) draw = orc_draw(key, e, l >> 1);
+      uint32_t u = (l & 1u) ? (uint32_t)(draw >> 32) : (uint32_t)draw;
+      s = (s << 1) | (u >= tab ? 1u : 0u);
+      d = (d << 1) | (((u >= ta && u < tab) || u >= tabc) ? 1u : 0u);
+    }
+    out[i * words] = s;
+    out[i * words + 1] = d;
+    if (weighted) out[i * words + 2] = orc_weight_bits(key, e);
+  }
+}
+
+uint64_t orc_grid_count(uint32_t n) { return n < 2 ? 0 : 4ull * n * (n - 1); }
+
+/* Records [first, first + count) of the n x n grid.  Rows r < n-1 hold
+ * 4n-2 records (4 per vertex, 2 for the last column), the last row 2(n-1). */
+void orc_grid_records(uint32_t n, uint64_t seed, int weighted, uint64_t first, uint64_t count,
+                      uint32_t *out) {
+  uint64_t key = orc_mix64(seed ^ 0x5851F42D4C957F2Dull);
+  int words = weighted ? 3 : 2;
+  uint64_t row_len = 4ull * n - 2;
+  for (uint64_t i = 0; i < count; i++) {
+    uint64_t e = first + i, r = e / row_len, k = e % row_len, c, slot;
+    if (r + 1 < n) {
+      c = k / 4;
+      slot = k % 4;
+      if (c + 1 == n) slot += 2;
+    } else {
+      c = k / 2;
+      slot = k % 2;
+    }
+    uint64_t v = r * n + c, a = v, b = slot < 2 ? v + 1 : v + n;
+    if (slot & 1) { uint64_t t = a; a = b; b = t; }
+    out[i * words] = (uint32_t)a;
+    out[i * words + 1] = (uint32_t)b;
+    if (weighted) out[i * words + 2] = orc_weight_bits(key, e);
+  }
+}
+
+/* deg[src] += 1 for every record (words = 2 or 3 per record). */
+void orc_count_out_degree(const uint32_t *rec, uint64_t n, int words, uint32_t *deg) {
+  for (uint64_t i = 0; i < n; i++) deg[rec[i * (uint64_t)words]] += 1;
+}
+
+/* Levels of a parent tree rooted at `root` (-1 unreached).  Returns 0, or -1
+ * when the root is not its own parent, a parent is out of range or
+ * unreached, or the array holds a cycle. */
+int orc_tree_levels(const uint32_t *parent, uint32_t V, uint32_t root, int32_t *level) {
+  if (root >= V || parent[root] != root) return -1;
+  for (uint32_t v = 0; v < V; v++) level[v] = parent[v] < V ? -2 : -1;  /* -2: reached, level unknown */
+  level[root] = 0;
+  uint32_t *stack = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(V ? V : 1));
+  int rc = 0;
+  for (uint32_t v = 0; v < V && rc == 0; v++) {
+    if (level[v] != -2) continue;
+    /* walk up to a vertex of known level, then assign on the way back */
+    uint32_t top = 0, u = v;
+    while (level[u] == -2) {
+      if (top >= V) { rc = -1; break; }     /* longer than V: a cycle */
+      stack[top++] = u;
+      level[u] = -3;                          /* on the current path */
+      u = parent[u];
+      if (u >= V) { rc = -1; break; }
+    }
+    if (rc) break;
+    if (level[u] < 0) { rc = -1; break; }    /* -3: cycle; -1: unreached parent */
+    int32_t base = level[u];
+    while (top > 0) level[stack[--top]] = ++base;
+  }
+  free(stack);
+  return rc;
+}

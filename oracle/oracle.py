@@ -40,6 +40,13 @@ def lib():
         L.orc_num_adj.argtypes = [vp]
         L.orc_num_adj.restype = u64
         L.orc_get_adj.argtypes = [vp, i32, vp, vp, vp, vp]
+        L.orc_rmat_records.argtypes = [u32, u64, i32, u64, u64, vp]
+        L.orc_grid_records.argtypes = [u32, u64, i32, u64, u64, vp]
+        L.orc_grid_count.argtypes = [u32]
+        L.orc_grid_count.restype = u64
+        L.orc_count_out_degree.argtypes = [vp, u64, i32, vp]
+        L.orc_tree_levels.argtypes = [vp, u32, u32, vp]
+        L.orc_tree_levels.restype = i32
         for name, extra in (("orc_bfs", [u32, vp]), ("orc_pagerank", [i32, vp, vp]), ("orc_cc", [vp]),
                             ("orc_sssp", [u32, vp]), ("orc_bc", [u32, vp, vp])):
             f = getattr(L, name)
@@ -183,4 +190,77 @@ def bfs_reference_levels(V, src, dst, root):
         nb = nb[level[nb] < 0]
         level[nb] = k
         frontier = nb
+    return level
+
+
+# ---------------------------------------------------------------- inputs
+RMAT, GRID = 0, 1
+
+
+def record_count(kind, p1, p2):
+    """Records of R-MAT (p1 = scale, p2 = edge factor) or of the p1 x p1 grid."""
+    return (1 << p1) * p2 if kind == RMAT else int(lib().orc_grid_count(p1))
+
+
+def records(kind, p1, p2, seed, weighted=False, first=0, count=None, threads=1):
+    """Packed edge-list records [first, first + count) as a uint32 array of
+    2 (3 when weighted) words per record, from the oracle's own restatement of
+    the benchmark generator (orc_rmat_records / orc_grid_records).  Threads
+    split the range; ctypes releases the GIL during each call."""
+    n = record_count(kind, p1, p2)
+    count = n - first if count is None else count
+    words = 3 if weighted else 2
+    out = np.empty(count * words, np.uint32)
+    fn = lib().orc_rmat_records if kind == RMAT else lib().orc_grid_records
+
+    def part(lo, hi):
+        if hi > lo:
+            fn(p1, seed, int(weighted), first + lo, hi - lo,
+               ctypes.c_void_p(out.ctypes.data + lo * words * 4))
+
+    threads = max(1, int(threads))
+    if threads == 1 or count < (1 << 16):
+        part(0, count)
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+        step = (count + threads - 1) // threads
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda i: part(i * step, min(count, (i + 1) * step)), range(threads)))
+    return out
+
+
+def write_records_file(path, kind, p1, p2, seed, weighted=False, threads=1, chunk=1 << 26):
+    """Writes the whole edge list to `path` chunk by chunk and returns
+    (vertices, records, out_degree uint32[V]) without holding the list."""
+    n = record_count(kind, p1, p2)
+    V = (1 << p1) if kind == RMAT else p1 * p1
+    words = 3 if weighted else 2
+    deg = np.zeros(V, np.uint32)
+    with open(path, "wb") as f:
+        for first in range(0, n, chunk):
+            c = min(chunk, n - first)
+            rec = records(kind, p1, p2, seed, weighted, first, c, threads)
+            lib().orc_count_out_degree(_ptr(rec), c, words, _ptr(deg))
+            rec.tofile(f)
+    return V, n, deg
+
+
+def pick_roots(out_degree, count, seed):
+    """Seeded uniform draws among the vertices with out-degree > 0: the
+    benchmark's root rule, restated so that the CPU baseline draws the GPU
+    run's roots without the product library."""
+    rng = np.random.default_rng(seed)
+    cand = np.nonzero(np.asarray(out_degree) > 0)[0]
+    if len(cand) == 0:
+        raise ValueError("no vertex with out-degree > 0")
+    return [int(x) for x in cand[rng.integers(0, len(cand), count)]]
+
+
+def tree_levels(parent, root):
+    """bfs_levels in C for large graphs: levels of the parent tree (-1
+    unreached); raises if the array is not a tree rooted at `root`."""
+    parent = np.ascontiguousarray(parent, np.uint32)
+    level = np.empty(len(parent), np.int32)
+    if lib().orc_tree_levels(_ptr(parent), len(parent), int(root), _ptr(level)) != 0:
+        raise AssertionError("parent array is not a tree rooted at %d" % root)
     return level

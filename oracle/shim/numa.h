@@ -13,6 +13,10 @@
  * full result arrays of a reference run can be compared with the oracle.
  * GG_REF_DUMP_MAX (default 64) bounds the number of dumps.
  * GG_REF_THREADS overrides the thread count the reference sees.
+ *
+ * A driver may also set gg_shim_free_observer to read each freed buffer
+ * (after the toolkit's timed region, before the unmap): oracle/ref_driver.cpp
+ * uses it to count the edges a BFS run traversed from its parent array.
  */
 #ifndef GG_SHIM_NUMA_H
 #define GG_SHIM_NUMA_H
@@ -67,8 +71,11 @@ static inline void *numa_realloc(void *old_addr, size_t old_size, size_t new_siz
   return p;
 }
 
+static void (*gg_shim_free_observer)(const void *start, size_t size) = 0;
+
 static inline void numa_free(void *start, size_t size) {
   static int seq = 0;
+  if (gg_shim_free_observer) gg_shim_free_observer(start, size);
   const char *dir = getenv("GG_REF_DUMP_DIR");
   const char *max_env = getenv("GG_REF_DUMP_MAX");
   int max_dumps = max_env ? atoi(max_env) : 64;

@@ -82,40 +82,45 @@ static uint64_t bm_count(const uint64_t *b, uint32_t V) {
   return c;
 }
 
-/* Stable counting sort of entry indices by key[] into order[]. */
-static void counting_sort(uint64_t n, const uint32_t *key, uint32_t V, const uint64_t *in_order,
-                          uint64_t *out_order, uint64_t *counts /* V+1 */) {
-  memset(counts, 0, sizeof(uint64_t) * ((size_t)V + 1));
-  for (uint64_t i = 0; i < n; i++) counts[key[in_order[i]] + 1] += 1;
-  for (uint32_t v = 0; v < V; v++) counts[v + 1] += counts[v];
-  for (uint64_t i = 0; i < n; i++) {
-    uint64_t e = in_order[i];
-    out_order[counts[key[e]]++] = e;
-  }
+static int cmp_u64(const void *a, const void *b) {
+  uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+  return x < y ? -1 : (x > y ? 1 : 0);
 }
 
 /* Builds one direction: entries grouped by major[], sorted by minor[], ties in
- * entry order (an LSD pass by minor, then by major). */
+ * entry order.  A stable counting pass groups the entries by major; each list
+ * is then sorted on (minor << 32 | position in the list), which keeps equal
+ * minors in entry order. */
 static void build_dir(uint32_t V, uint64_t n, const uint32_t *major, const uint32_t *minor,
                       const float *w, uint64_t **off_out, uint32_t **nbr_out, float **w_out) {
-  uint64_t *a = (uint64_t *)malloc(sizeof(uint64_t) * (n ? n : 1));
-  uint64_t *b = (uint64_t *)malloc(sizeof(uint64_t) * (n ? n : 1));
-  uint64_t *counts = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)V + 1));
-  for (uint64_t i = 0; i < n; i++) a[i] = i;
-  counting_sort(n, minor, V, a, b, counts);
-  counting_sort(n, major, V, b, a, counts);
   uint64_t *off = (uint64_t *)calloc((size_t)V + 1, sizeof(uint64_t));
   for (uint64_t i = 0; i < n; i++) off[major[i] + 1] += 1;
   for (uint32_t v = 0; v < V; v++) off[v + 1] += off[v];
+  uint64_t *fill = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)V + 1));
+  memcpy(fill, off, sizeof(uint64_t) * ((size_t)V + 1));
+  uint64_t *order = (uint64_t *)malloc(sizeof(uint64_t) * (n ? n : 1));
+  for (uint64_t i = 0; i < n; i++) order[fill[major[i]]++] = i;
+  free(fill);
   uint32_t *nbr = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
   float *ww = w ? (float *)malloc(sizeof(float) * (n ? n : 1)) : NULL;
-  for (uint64_t i = 0; i < n; i++) {
-    nbr[i] = minor[a[i]];
-    if (ww) ww[i] = w[a[i]];
+  uint64_t *keys = NULL;
+  uint64_t cap = 0;
+  for (uint32_t v = 0; v < V; v++) {
+    uint64_t lo = off[v], len = off[v + 1] - lo;
+    if (len > cap) {
+      cap = len;
+      keys = (uint64_t *)realloc(keys, sizeof(uint64_t) * cap);
+    }
+    for (uint64_t k = 0; k < len; k++) keys[k] = ((uint64_t)minor[order[lo + k]] << 32) | k;
+    if (len > 1) qsort(keys, len, sizeof(uint64_t), cmp_u64);
+    for (uint64_t k = 0; k < len; k++) {
+      uint64_t e = order[lo + (keys[k] & 0xFFFFFFFFull)];
+      nbr[lo + k] = minor[e];
+      if (ww) ww[lo + k] = w[e];
+    }
   }
-  free(a);
-  free(b);
-  free(counts);
+  free(keys);
+  free(order);
   *off_out = off;
   *nbr_out = nbr;
   *w_out = ww;
@@ -456,7 +461,11 @@ int orc_sssp(const orc_graph *g, uint32_t root, float *dist, orc_trace *tr) {
 /* toolkits/bc.cpp:24-196 (compute; COMPACT = 0).  dep receives
  * `dependencies`, inv receives `inv_num_paths` (the array the toolkit frees
  * last, bc.cpp:192-193). */
-int orc_bc(orc_graph *g, uint32_t root, double *dep, double *inv, orc_trace *tr) {
+int orc_bc(const orc_graph *g0, uint32_t root, double *dep, double *inv, orc_trace *tr) {
+  /* transpose() acts on a private copy of the handles, so that several
+   * threads may run BC on one graph */
+  orc_graph gl = *g0;
+  orc_graph *g = &gl;
   uint32_t V = g->V;
   if (root >= V) return -1;
   size_t words = (size_t)V / 64 + 1;
@@ -695,4 +704,21 @@ int orc_tree_levels(const uint32_t *parent, uint32_t V, uint32_t root, int32_t *
   }
   free(stack);
   return rc;
+}
+
+/* Number of reached vertices v != root whose tree edge (parent[v], v) is not
+ * an edge of the graph (in-lists are sorted by neighbour id). */
+uint64_t orc_tree_bad_edges(const orc_graph *g, const uint32_t *parent, uint32_t root) {
+  uint64_t bad = 0;
+  for (uint32_t v = 0; v < g->V; v++) {
+    uint32_t p = parent[v];
+    if (v == root || p >= g->V) continue;
+    uint64_t lo = g->in_off[v], hi = g->in_off[v + 1];
+    while (lo < hi) {
+      uint64_t mid = lo + (hi - lo) / 2;
+      if (g->in_nbr[mid] < p) lo = mid + 1; else hi = mid;
+    }
+    if (lo == g->in_off[v + 1] || g->in_nbr[lo] != p) bad++;
+  }
+  return bad;
 }

@@ -47,6 +47,8 @@ def lib():
         L.orc_count_out_degree.argtypes = [vp, u64, i32, vp]
         L.orc_tree_levels.argtypes = [vp, u32, u32, vp]
         L.orc_tree_levels.restype = i32
+        L.orc_tree_bad_edges.argtypes = [vp, vp, u32]
+        L.orc_tree_bad_edges.restype = u64
         for name, extra in (("orc_bfs", [u32, vp]), ("orc_pagerank", [i32, vp, vp]), ("orc_cc", [vp]),
                             ("orc_sssp", [u32, vp]), ("orc_bc", [u32, vp, vp])):
             f = getattr(L, name)
@@ -133,6 +135,11 @@ class OracleGraph:
         if rc < 0:
             raise ValueError("bad root or unweighted graph")
         return dist, tr.rows()
+
+    def tree_bad_edges(self, parent, root):
+        """Reached vertices whose parent edge is not an edge of this graph."""
+        parent = np.ascontiguousarray(parent, np.uint32)
+        return int(lib().orc_tree_bad_edges(self.h, _ptr(parent), int(root)))
 
     def bc(self, root):
         dep = np.zeros(self.V, np.float64)

@@ -105,6 +105,7 @@ def library():
         "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_pr_layout": ([vp, i32], i32),
+        "gg_graph_set_l1_hot": ([vp, u32], i32),
         "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
@@ -332,6 +333,11 @@ class Graph:
 
     def set_pr_layout(self, hot_sources):
         _check(library().gg_graph_set_pr_layout(self.h, 1 if hot_sources else 0))
+
+    def set_l1_hot(self, l1_bytes):
+        """Bytes of the most gathered sources' state the pulls cache in L1 on
+        the hot-source layout (gg_graph_set_l1_hot)."""
+        _check(library().gg_graph_set_l1_hot(self.h, int(l1_bytes)))
 
     def autotune(self, cache_dir=None, objective=("pagerank", "bfs")):
         """Times the bin candidates on this graph for the named workloads

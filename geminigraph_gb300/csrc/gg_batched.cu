@@ -1128,7 +1128,7 @@ static int run_batch(gg_graph *g, LanePool::Kind kind, const uint32_t *roots, in
   int status = GG_OK;
   LanePool *p = graph_pool(g, kind, parents, &status);
   if (status != GG_OK) return status;
-  Trace tr(stats, g);
+  Trace tr(stats, g, kind == LanePool::BFS ? "gg_bfs_batched" : "gg_sssp_batched");
   p->set_trace(&tr);
   p->launches = 0;
   const uint32_t V = g->V;

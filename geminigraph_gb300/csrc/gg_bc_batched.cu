@@ -382,7 +382,7 @@ static int bc_batched_run(gg_graph *g, const uint32_t *roots, int n, double *dep
     *out = (u64 *)levels.back().p;
     return GG_OK;
   };
-  Trace tr(st, g);
+  Trace tr(st, g, "gg_bc_batched");
   int launches = 0;
   GG_CUDA(cudaMemcpyAsync(roots_b.p, roots, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
   GG_TRY(timed_begin(g));

@@ -52,7 +52,7 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
   GG_TRY(ws(g, WS_Q0, (size_t)V + 1, &q[0]));
   GG_TRY(ws(g, WS_Q1, (size_t)V + 1, &q[1]));
   Launch L(g);
-  Trace tr(st, g);
+  Trace tr(st, g, "gg_bfs");
   cudaStream_t s = g->stream;
   Counters *ctr = g->ws.ctr;
   GG_TRY(timed_begin(g));
@@ -139,10 +139,13 @@ struct PrPull {
   T *next;
   const uint32_t *out_deg;
   int last;
+  uint32_t hot = 0xffffffffu;  // sources below this number are gathered through L1
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
   __device__ __forceinline__ T identity(uint32_t) const { return T(0); }
   __device__ __forceinline__ T identity_coop() const { return T(0); }
-  __device__ __forceinline__ T gather(const Dir &, unsigned long long, uint32_t u) const { return curr[u]; }
+  __device__ __forceinline__ T gather(const Dir &, unsigned long long, uint32_t u) const {
+    return ld_gather(curr, u, hot);
+  }
   __device__ __forceinline__ T combine(T a, T b) const { return a + b; }
   __device__ __forceinline__ T warp_combine(T x) const { return warp_sum(x); }
   __device__ __forceinline__ bool finish(uint32_t v, T sum, uint32_t, Tally &t) const;
@@ -221,7 +224,7 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
   GG_TRY(ws(g, WS_S3, (size_t)V, &buf[1]));
   GG_TRY(ws(g, WS_HUBSUM, (size_t)(iterations > 0 ? iterations : 1), &per_iter));
   Launch L(g);
-  Trace tr(st, g);
+  Trace tr(st, g, "gg_pagerank");
   cudaStream_t s = g->stream;
   GG_TRY(timed_begin(g));
   GG_CUDA(cudaMemsetAsync(per_iter, 0, sizeof(Counters) * (iterations > 0 ? iterations : 1), s));
@@ -232,7 +235,8 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
   unsigned long long ae = g->nadj;
   for (int i = 0; i < iterations; i++) {
     tr.add(ae < g->E / 20 ? 0 : 1, ae, V);
-    PrPull<T> op{buf[cur], buf[cur ^ 1], od, i == iterations - 1};
+    PrPull<T> op{buf[cur], buf[cur ^ 1], od, i == iterations - 1,
+                 ranked ? (uint32_t)(g->l1_hot_bytes / sizeof(T)) : 0xffffffffu};
     GG_TRY(tr.kbegin());
     GG_TRY(L.pull(din, op, ActOut(), per_iter + i));
     GG_TRY(tr.kend());
@@ -300,6 +304,15 @@ int gg_graph_set_pr_layout(gg_graph *g, int hot_sources) {
   }
   g->pr_layout = hot_sources ? 1 : 0;
   if (!g->pr_layout) pr_layout_free(g);
+  return GG_OK;
+}
+
+int gg_graph_set_l1_hot(gg_graph *g, uint32_t l1_bytes) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  g->l1_hot_bytes = l1_bytes;
   return GG_OK;
 }
 
@@ -392,6 +405,7 @@ int gg_active_edges(gg_graph *g, const uint64_t *active_bitmap, uint64_t *active
     return GG_ERR_INVALID;
   }
   GG_CUDA(cudaSetDevice(g->device));
+  Trace range(nullptr, g, "process_vertices");
   size_t words = bitmap_words32(g->V);
   uint32_t *bm;
   GG_TRY(ws(g, WS_BM3, words, &bm));

@@ -29,10 +29,13 @@ struct CcPull {
   const uint32_t *cur;
   uint32_t *nxt;
   const uint32_t *ids = nullptr;  // hot-source layout: vertex id of each rank (the message starts at dst's id)
+  uint32_t hot = 0xffffffffu;     // sources below this number are gathered through L1
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
   __device__ __forceinline__ uint32_t identity(uint32_t v) const { return ids ? ids[v] : v; }
   __device__ __forceinline__ uint32_t identity_coop() const { return 0xffffffffu; }
-  __device__ __forceinline__ uint32_t gather(const Dir &, unsigned long long, uint32_t u) const { return cur[u]; }
+  __device__ __forceinline__ uint32_t gather(const Dir &, unsigned long long, uint32_t u) const {
+    return ld_gather(cur, u, hot);
+  }
   __device__ __forceinline__ uint32_t combine(uint32_t a, uint32_t b) const { return b < a ? b : a; }
   __device__ __forceinline__ uint32_t warp_combine(uint32_t x) const { return warp_min(x); }
   __device__ __forceinline__ bool finish(uint32_t v, uint32_t m, uint32_t, Tally &) const {
@@ -76,11 +79,12 @@ struct SsspPull {
   using Acc = float;
   const float *cur;
   float *nxt;
+  uint32_t hot = 0xffffffffu;  // sources below this number are gathered through L1
   __device__ __forceinline__ bool want(uint32_t) const { return true; }
   __device__ __forceinline__ float identity(uint32_t) const { return 1e9f; }
   __device__ __forceinline__ float identity_coop() const { return 1e9f; }
   __device__ __forceinline__ float gather(const Dir &d, unsigned long long k, uint32_t u) const {
-    return __fadd_rn(cur[u], d.w[k]);
+    return __fadd_rn(ld_gather(cur, u, hot), d.w[k]);
   }
   __device__ __forceinline__ float combine(float a, float b) const { return b < a ? b : a; }
   __device__ __forceinline__ float warp_combine(float x) const { return warp_min(x); }
@@ -201,7 +205,7 @@ static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   uint32_t *out = nullptr;
   if (ranked) GG_TRY(ws(g, WS_S2, V, &out));
   Launch L(g);
-  Trace tr(st, g);
+  Trace tr(st, g, "gg_cc");
   cudaStream_t s = g->stream;
   GG_TRY(timed_begin(g));
   // label[v] = v over active_in = all (cc.cpp:31-37)
@@ -215,6 +219,7 @@ static int cc_run(gg_graph *g, uint32_t *label_host, gg_run_stats *st) {
   uint32_t *res = nullptr;
   CcPull pull{};
   pull.ids = ranked ? g->pr_id_of_rank : nullptr;
+  pull.hot = ranked ? g->l1_hot_bytes / 4 : 0xffffffffu;
   GG_TRY((relax_loop<uint32_t, CcPush, CcPull>(g, dout, din, pull, lab[0], lab[1], q[0], q[1], bm[0], bm[1], V, 0,
                                                0xffffffffu, false, g->nadj, tr, L, &res)));
   if (ranked) {
@@ -279,7 +284,7 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
     GG_TRY(ws(g, WS_S2, V, &out));
   }
   Launch L(g);
-  Trace tr(st, g);
+  Trace tr(st, g, "gg_sssp");
   cudaStream_t s = g->stream;
   GG_TRY(timed_begin(g));
   GG_CUDA(cudaMemsetAsync(bm[0], 0, words * 4, s));
@@ -291,7 +296,9 @@ static int sssp_run(gg_graph *g, uint32_t root, float *dist_host, gg_run_stats *
   Counters c;
   GG_TRY(counters_read(g, &c));
   float *res = nullptr;
-  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dout, din, SsspPull{}, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1,
+  SsspPull pull{};
+  pull.hot = ranked ? g->l1_hot_bytes / 4 : 0xffffffffu;
+  GG_TRY((relax_loop<float, SsspPush, SsspPull>(g, dout, din, pull, dist[0], dist[1], q[0], q[1], bm[0], bm[1], 1,
                                                 1, c.maxdeg, true, c.edges, tr, L, &res)));
   if (ranked) {
     unrank<float><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(res, g->pr_rank_of, V, out);
@@ -441,7 +448,7 @@ static int bc_run(gg_graph *g, uint32_t root, double *dep_host, double *inv_host
     GG_TRY(ws(g, WS_S1, V, &np_out));
   }
   Launch L(g);
-  Trace tr(st, g);
+  Trace tr(st, g, "gg_bc");
   cudaStream_t s = g->stream;
   Counters *ctr = g->ws.ctr;
   GG_TRY(timed_begin(g));

@@ -16,6 +16,7 @@
 #define GG_COMMON_CUH
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -172,6 +173,9 @@ struct gg_graph {
   uint32_t batched_switch_div = 20;
   int wmin_known = 0;
   float wmin = 0.0f;
+  // reduction pulls on the hot-source layout: gathered state of the first
+  // l1_hot_bytes worth of sources is cached in L1, the rest read past it
+  uint32_t l1_hot_bytes = 160u << 10;
 };
 
 namespace gg {
@@ -207,12 +211,24 @@ size_t scan_scratch_elems(size_t n);
 
 // Stats/trace helper for toolkits: one row per process_edges call, and, when
 // the caller passed call_ms, CUDA events around each call's edge kernel.
+// Per-call record of a toolkit run (the process_edges trace), and the NVTX
+// ranges a profiler cuts the run by: one range named after the run (when a
+// name is given), and
+// inside it one range per process_edges call ("process_edges sparse" or
+// "process_edges dense", payload = the call's active_edges), which holds the
+// call's kernel launches.  Calls that a cooperative small-run launch
+// executes on the device are recorded after it and get empty ranges.
 struct Trace {
   gg_run_stats *st;
   gg_graph *g;
   std::vector<int> ev_call;
   std::vector<cudaEvent_t> ev;
-  Trace(gg_run_stats *s, gg_graph *gr) : st(s), g(gr) {
+  int nvtx_depth = 0;
+  Trace(gg_run_stats *s, gg_graph *gr, const char *run = nullptr) : st(s), g(gr) {
+    if (run) {
+      nvtxRangePushA(run);
+      nvtx_depth = 1;
+    }
     if (st) {
       st->calls = 0;
       st->active_edges_total = 0;
@@ -220,7 +236,31 @@ struct Trace {
       st->kernel_launches = 0;
     }
   }
+  ~Trace() {
+    for (; nvtx_depth > 0; nvtx_depth--) nvtxRangePop();
+  }
+  Trace(const Trace &) = delete;
+  Trace &operator=(const Trace &) = delete;
+  void call_range(int mode, uint64_t active_edges) {
+    if (nvtx_depth == 0) return;
+    if (nvtx_depth == 2) {
+      nvtxRangePop();
+      nvtx_depth = 1;
+    }
+    nvtxEventAttributes_t a = {};
+    a.version = NVTX_VERSION;
+    a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+    a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+    a.message.ascii = mode ? "process_edges dense" : "process_edges sparse";
+    a.payloadType = NVTX_PAYLOAD_TYPE_UNSIGNED_INT64;
+    a.payload.ullValue = active_edges;
+    if (nvtx_depth == 1) {
+      nvtxRangePushEx(&a);
+      nvtx_depth = 2;
+    }
+  }
   void add(int mode, uint64_t active_edges, uint64_t activated) {
+    call_range(mode, active_edges);
     if (!st) return;
     int i = st->calls;
     if (i < st->trace_capacity) {
@@ -282,6 +322,32 @@ __device__ __forceinline__ uint32_t ld_once(const uint32_t *p) {
   uint32_t v;
   asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
   return v;
+}
+__device__ __forceinline__ uint4 ld_once_v4(const uint32_t *p) {
+  uint4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ld_once(const float *p) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_once(const double *p) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// A gathered value of vertex state: the first `hot` entries (on the
+// hot-source layout, the most gathered sources) are cached in L1; the rest
+// are read past L1, so that they do not evict the hot entries.  The state
+// was written by an earlier kernel, so the read-only path is safe.
+template <typename T>
+__device__ __forceinline__ T ld_gather(const T *a, uint32_t u, uint32_t hot) {
+  return u < hot ? __ldg(a + u) : ld_once(a + u);
 }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 

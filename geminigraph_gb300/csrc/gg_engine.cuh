@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
 // flight per lane; partials[c] = the chunk's combine (lane order, then the
 // warp tree).  Two load shapes (d.vec, picked per graph by the autotuner):
 //   VEC    lane l loads the block's 16-byte windows l, l + 32, ... with one
-//          vector load each (fewer load instructions);
+//          vector load each (fewer load instructions), read past L1;
 //   !VEC   lane l takes entries l, l + 32, ... (a warp's gathers touch
 //          consecutive entries, which share cache sectors where an in-list
 //          holds runs of consecutive source numbers), read past L1.
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(PULL_THREADS)
 #pragma unroll
         for (int i = 0; i < WIN; i++) {
           const unsigned long long p = lo + 4 * (lane + 32 * i);
-          w[i] = p < e && p + 4 > b ? __ldg(reinterpret_cast<const uint4 *>(d.nbr + p)) : make_uint4(0, 0, 0, 0);
+          w[i] = p < e && p + 4 > b ? ld_once_v4(d.nbr + p) : make_uint4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int i = 0; i < WIN; i++) {

@@ -363,6 +363,15 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
  * identical either way, BC dependencies equal up to summation order. */
 int gg_graph_set_pr_layout(gg_graph *g, int hot_sources);
 
+/* Cache policy of the reduction pulls on that layout (no reference
+ * counterpart: the reference's gathers go through the CPU caches).  The
+ * gathered state of the first l1_bytes worth of sources -- the most gathered
+ * ones -- is cached in each SM's L1, and every other gather is read past L1 so
+ * that it does not evict them.  0 reads every gather past L1; a value at least
+ * the whole state array caches every gather (the plain layout always does).
+ * Results do not depend on it.  Default 163840 (160 KiB). */
+int gg_graph_set_l1_hot(gg_graph *g, uint32_t l1_bytes);
+
 /* ---- engine primitives ---- */
 
 /* Graph::process_vertices (core/graph.hpp:1406-1469) for the reduction

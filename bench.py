@@ -477,14 +477,17 @@ def tune_bins(g, args):
     """Degree bins for this graph: the library defaults, or the autotuner's
     pick for the workload's kernels (timed on the graph, cached on disk)."""
     if args.bins == "default":
-        return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1}
+        return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1, "l1_hot_bytes": None}
     objective = ("pagerank",) if args.workload.startswith("pagerank") else \
         ("batched",) if args.workload in ("bfs_batched", "sssp_batched", "bc_batched", "serve") else \
-        ("bfs",) if args.workload.startswith("bfs") else ("pagerank", "bfs")
+        ("bfs",) if args.workload.startswith("bfs") else ("sssp",) if args.workload == "sssp" else \
+        ("cc",) if args.workload == "cc" else ("pagerank", "bfs")
     t0 = time.perf_counter()
     r = g.autotune(objective=objective)
     return {"source": "autotune(%s)" % "+".join(objective), "light_deg": r["light_deg"],
-            "pull_chunk": r["pull_chunk"], "pull_vector": r["pull_vector"], "from_cache": bool(r["from_cache"]),
+            "pull_chunk": r["pull_chunk"], "pull_vector": r["pull_vector"],
+            "l1_hot_bytes": None if r["l1_hot_bytes"] == 0xffffffff else r["l1_hot_bytes"],
+            "from_cache": bool(r["from_cache"]),
             "tune_s": round(time.perf_counter() - t0, 2),
             "objective_ms_default": round(r["default_ms"], 3), "objective_ms_chosen": round(r["best_ms"], 3)}
 
@@ -512,7 +515,6 @@ def gpu_arm(args, dist):
     wall0 = time.perf_counter()
     for a in step_in[args.warmup:n]:
         st = gg.RunStats()
-        st.enable_call_timing()
         stats.append(run_once_stats(gg, g, args.workload, a, st))
     wall = time.perf_counter() - wall0
     dist.barrier()
@@ -523,10 +525,17 @@ def gpu_arm(args, dist):
     t_max = dist.max(dev_ms / 1000.0)
     edges_all = dist.sum(edges)
     value = edges_all / t_max / 1e9
-    # ---- dominant kernel roofline
+    # ---- dominant kernel roofline: the first timed steps again, with CUDA
+    # events around every process_edges call (events between the kernels
+    # would slow the timed steps above, and break up PageRank's captured graph)
+    tstats = []
+    for a in step_in[args.warmup:n][:5]:
+        st = gg.RunStats()
+        st.enable_call_timing()
+        tstats.append(run_once_stats(gg, g, args.workload, a, st))
     per_mode = {0: [0.0, 0.0, 0, 0], 1: [0.0, 0.0, 0, 0]}   # ms, bytes, launches, adjacency bytes
     adj_per_edge = 8 if w["weighted"] else 4
-    for s in stats:
+    for s in tstats:
         prev_act = 1
         for i, (mode, ae, act) in enumerate(s.rows()):
             ms = float(s.call_ms[i])
@@ -550,6 +559,8 @@ def gpu_arm(args, dist):
                 # below frac where pull-mode BFS skips counted edges
                 "dram_frac": round(traffic / (avg_ms / 1000.0) / 1e9 / peak, 4) if traffic and avg_ms > 0 else None,
                 "launches": per_mode[dom][2],
+                "timed_in": "per-call CUDA events on the library's stream, a second pass over the first "
+                            f"{len(tstats)} timed roots",
                 "avg_launch_ms": round(per_mode[dom][0] / max(per_mode[dom][2], 1), 4),
                 "share_of_edge_kernel_time": round(per_mode[dom][0] / total_kernel_ms, 4) if total_kernel_ms else None}
     # ---- e2e through the C ABI with host buffers
@@ -601,8 +612,8 @@ def gpu_arm(args, dist):
                      "d2h_bytes_per_step": d2h, "ms_per_step": round(e_max * 1000 / args.steps, 3)}, **e2e_extra),
         "roofline": roofline,
         "gpu_launches": launches,
-        "trace_first_step": [[m, ae, act, round(float(stats[0].call_ms[i]), 4)]
-                             for i, (m, ae, act) in enumerate(stats[0].rows()[:40])] if stats else [],
+        "trace_first_step": [[m, ae, act, round(float(tstats[0].call_ms[i]), 4)]
+                             for i, (m, ae, act) in enumerate(tstats[0].rows()[:40])] if tstats else [],
         "wall_s": round(wall, 3),
         "clocks": clk,
     }
@@ -654,14 +665,14 @@ def gpu_arm_batched(args, dist):
 
     bc = args.workload == "bc_batched"
 
-    def run_batch(rs, host):
+    def run_batch(rs, host, timing=False):
         if bfs:
-            _, _, _, edges, st = gg.bfs_batched(g, rs, levels=host, parents=False, timing=True)
+            _, _, _, edges, st = gg.bfs_batched(g, rs, levels=host, parents=False, timing=timing)
             return st, int(edges.sum())
         if bc:
-            _, _, _, st = gg.bc_batched(g, rs, outputs=host, timing=True)
+            _, _, _, st = gg.bc_batched(g, rs, outputs=host, timing=timing)
             return st, 0
-        _, _, st = gg.sssp_batched(g, rs, distances=host, timing=True)
+        _, _, st = gg.sssp_batched(g, rs, distances=host, timing=timing)
         return st, 0
 
     for b in batches[:args.warmup]:
@@ -676,9 +687,10 @@ def gpu_arm_batched(args, dist):
         dev_ms += st.device_ms
         edges += e
         launches += st.kernel_launches
-        first = first or st
     dist.barrier()
     clk = clocks.stop()
+    # per-step kernel times of the first batch, in a pass of its own
+    first = run_batch(batches[args.warmup], False, timing=True)[0]
     t_max = dist.max(dev_ms / 1000.0)
     q_all = dist.sum(lanes * args.steps)
     value = q_all / t_max
@@ -891,7 +903,8 @@ def gpu_arm_serve(args, dist):
         "data": "synthetic (seeded R-MAT generated on the device; Poisson query stream)",
         "config": {"workload": WORKLOADS["serve"]["desc"], "queries": n, "rate_qps": args.rate,
                    "graph_build_s": round(build_s, 2), "parallelism": f"replicas x{args.gpus}",
-                   "bins": [{k: b[k] for k in ("source", "light_deg", "pull_chunk", "pull_vector")} for b in bins]},
+                   "bins": [{k: b[k] for k in ("source", "light_deg", "pull_chunk", "pull_vector", "l1_hot_bytes")}
+                            for b in bins]},
         "latency_ms": {"p50": round(pct(lat, 50), 3), "p99": round(pct(lat, 99), 3)},
         "plain": {"value": round(plain_qps, 1) if plain_qps else None, "unit": "queries/s",
                   "latency_ms": {"p50": round(pct(plain_lat, 50), 3), "p99": round(pct(plain_lat, 99), 3)},

@@ -106,6 +106,7 @@ def library():
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_pr_layout": ([vp, i32], i32),
         "gg_graph_set_l1_hot": ([vp, u32], i32),
+        "gg_graph_set_dense_push": ([vp, u32], i32),
         "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
@@ -142,7 +143,8 @@ class _ServerStats(ctypes.Structure):
 class _TuneResult(ctypes.Structure):
     _fields_ = [("light_deg", ctypes.c_uint32), ("pull_chunk", ctypes.c_uint32), ("pull_vector", ctypes.c_uint32),
                 ("best_ms", ctypes.c_double),
-                ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32)]
+                ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32),
+                ("l1_hot_bytes", ctypes.c_uint32)]
 
 
 class RunStats:
@@ -339,11 +341,19 @@ class Graph:
         the hot-source layout (gg_graph_set_l1_hot)."""
         _check(library().gg_graph_set_l1_hot(self.h, int(l1_bytes)))
 
+    def set_dense_push(self, divisor):
+        """CC / SSSP dense calls with active out-edges below adjacency
+        entries / divisor run as a push (0: always pull)."""
+        _check(library().gg_graph_set_dense_push(self.h, int(divisor)))
+
     def autotune(self, cache_dir=None, objective=("pagerank", "bfs")):
         """Times the bin candidates on this graph for the named workloads
-        ("pagerank", "bfs", "batched") and keeps the fastest; cached on disk."""
-        mask = (1 if "pagerank" in objective else 0) | (2 if "bfs" in objective else 0) | \
-            (4 if "batched" in objective else 0)
+        ("pagerank", "bfs", "batched", "sssp", "cc") and keeps the fastest;
+        cached on disk."""
+        names = {"pagerank": 1, "bfs": 2, "batched": 4, "sssp": 8, "cc": 16}
+        mask = 0
+        for o in objective:
+            mask |= names[o]
         r = _TuneResult()
         _check(library().gg_autotune(self.h, mask, os.fsencode(cache_dir) if cache_dir else None, ctypes.byref(r)))
         return {k: getattr(r, k) for k, _ in _TuneResult._fields_}

@@ -226,29 +226,82 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
   Launch L(g);
   Trace tr(st, g, "gg_pagerank");
   cudaStream_t s = g->stream;
-  GG_TRY(timed_begin(g));
-  GG_CUDA(cudaMemsetAsync(per_iter, 0, sizeof(Counters) * (iterations > 0 ? iterations : 1), s));
-  pr_init<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[0], od, V);
-  L.launches += 1;
+  const uint32_t hot = ranked ? (uint32_t)(g->l1_hot_bytes / sizeof(T)) : 0xffffffffu;
+  T *part = nullptr;
+  if (din.nbig) GG_TRY(ws(g, WS_PARTIAL, din.nbigchunks, &part));
+  // The run is device work only, so it is captured once as a CUDA graph and
+  // replayed while its arguments are unchanged: no launch gaps between the
+  // iterations' kernels.
+  PrGraphKey key;
+  memset(&key, 0, sizeof(key));
+  key.din = din;
+  key.od = od;
+  key.buf0 = buf[0];
+  key.buf1 = buf[1];
+  key.out = out;
+  key.per_iter = per_iter;
+  key.partial = part;
+  key.V = V;
+  key.iterations = iterations;
+  key.tsize = (int32_t)sizeof(T);
+  key.ranked = ranked;
+  key.timing = tr.timing_requested();
+  key.hot = hot;
+  key.side = g->side;
+  const int slot = sizeof(T) == 4 ? 0 : 1;  // one cached graph per precision
+  cudaGraphExec_t &exec = g->pr_exec[slot];
+  const bool replay = exec && memcmp(&key, &g->pr_key[slot], sizeof(key)) == 0;
   int cur = 0;
-  // active = all: active_edges = sum of out_degree = adjacency entries
-  unsigned long long ae = g->nadj;
-  for (int i = 0; i < iterations; i++) {
-    tr.add(ae < g->E / 20 ? 0 : 1, ae, V);
-    PrPull<T> op{buf[cur], buf[cur ^ 1], od, i == iterations - 1,
-                 ranked ? (uint32_t)(g->l1_hot_bytes / sizeof(T)) : 0xffffffffu};
-    GG_TRY(tr.kbegin());
-    GG_TRY(L.pull(din, op, ActOut(), per_iter + i));
-    GG_TRY(tr.kend());
-    GG_CUDA(cudaGetLastError());
-    cur ^= 1;
-  }
-  const T *result = buf[cur];
-  if (ranked) {
-    pr_unrank<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[cur], g->pr_rank_of, V, out);
+  // bookkeeping (trace, launch count) always; launches only while capturing
+  auto enqueue = [&](bool launch) -> int {
+    if (launch) {
+      GG_CUDA(cudaMemsetAsync(per_iter, 0, sizeof(Counters) * (iterations > 0 ? iterations : 1), s));
+      pr_init<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[0], od, V);
+    }
     L.launches += 1;
-    result = out;
+    cur = 0;
+    // active = all: active_edges = sum of out_degree = adjacency entries
+    unsigned long long ae = g->nadj;
+    for (int i = 0; i < iterations; i++) {
+      tr.add(ae < g->E / 20 ? 0 : 1, ae, V);
+      PrPull<T> op{buf[cur], buf[cur ^ 1], od, i == iterations - 1, hot};
+      GG_TRY(tr.kbegin());
+      if (launch)
+        GG_TRY(L.pull(din, op, ActOut(), per_iter + i));
+      else
+        L.launches += Launch::pull_launches(din);
+      GG_TRY(tr.kend());
+      cur ^= 1;
+    }
+    if (ranked) {
+      if (launch) pr_unrank<T><<<grid_for(V, 256, g->num_sms), 256, 0, s>>>(buf[cur], g->pr_rank_of, V, out);
+      L.launches += 1;
+    }
+    if (launch) GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  };
+  if (!replay) {
+    if (exec) GG_CUDA(cudaGraphExecDestroy(exec));
+    exec = nullptr;
+    GG_TRY(tr.reserve_events(2 * (size_t)iterations));
+    GG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    tr.capturing = true;
+    const int rc = enqueue(true);
+    tr.capturing = false;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc == GG_OK && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc != GG_OK) return rc;
+    GG_CUDA(e);
+    g->pr_key[slot] = key;
+  } else {
+    tr.replay = true;
+    GG_TRY(enqueue(false));
   }
+  GG_TRY(timed_begin(g));
+  GG_CUDA(cudaGraphLaunch(exec, s));
+  const T *result = ranked ? out : buf[cur];
   GG_TRY(timed_end(g, st, L.launches));
   GG_TRY(tr.collect());
   if (deltas_host && iterations > 0) {
@@ -313,6 +366,15 @@ int gg_graph_set_l1_hot(gg_graph *g, uint32_t l1_bytes) {
     return GG_ERR_INVALID;
   }
   g->l1_hot_bytes = l1_bytes;
+  return GG_OK;
+}
+
+int gg_graph_set_dense_push(gg_graph *g, uint32_t divisor) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  g->dense_push_div = divisor;
   return GG_OK;
 }
 

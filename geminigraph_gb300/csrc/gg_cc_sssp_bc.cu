@@ -128,17 +128,24 @@ static int relax_loop(gg_graph *g, const Dir &dout, const Dir &din, const PullOp
       continue;
     }
     tr.add(sparse ? 0 : 1, ae, 0);
+    // A dense call may run as a push over the frontier: a source that is
+    // not active was relaxed against its current value in the call after it
+    // last changed, so it cannot lower any out-neighbour now, and the
+    // minimum over the active sources' candidates is the dense call's
+    // minimum over all in-edges -- the same values and the same activated
+    // set (the snapshot keeps every signal before every slot).
+    const bool push = sparse || (g->dense_push_div && ae < g->nadj / g->dense_push_div);
     int nx = c_i ^ 1;
-    if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[c_i], dout.nz, q[c_i], &nq));
+    if (push && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[c_i], dout.nz, q[c_i], &nq));
     GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
     GG_TRY(counters_reset(g));
     ActOut a;
     a.active_out = bm[nx];
-    a.q_out = sparse ? q[nx] : nullptr;
+    a.q_out = push ? q[nx] : nullptr;
     a.qlen = &ctr->qlen;
     a.out_deg = dout.deg;
     a.queue_nonzero_only = true;
-    if (sparse) {
+    if (push) {
       if (ae > 0) {
         gather_by_queue<T><<<grid_for(nq, 256, g->num_sms), 256, 0, s>>>(q[c_i], nq, cur, msg);
         unsigned long long *P;
@@ -166,7 +173,7 @@ static int relax_loop(gg_graph *g, const Dir &dout, const Dir &din, const PullOp
     n_act = c.activated;
     nq = c.qlen;
     md = c.maxdeg;
-    qvalid = sparse;
+    qvalid = push;
     ae = c.edges;
     tr.set_activated(c.activated);
     c_i = nx;

@@ -128,6 +128,18 @@ void pr_layout_free(gg_graph *g);
 
 }  // namespace gg
 
+// Everything the launches of a captured PageRank run depend on: the kernels'
+// arguments and grids, the buffers and events.  A run whose key equals the
+// cached one replays the cached CUDA graph.
+struct PrGraphKey {
+  gg::Dir din;
+  const void *od, *buf0, *buf1, *out, *per_iter, *partial;
+  uint32_t V;
+  int32_t iterations, tsize, ranked, timing;
+  uint32_t hot;
+  cudaStream_t side;
+};
+
 struct gg_graph {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -175,7 +187,16 @@ struct gg_graph {
   float wmin = 0.0f;
   // reduction pulls on the hot-source layout: gathered state of the first
   // l1_hot_bytes worth of sources is cached in L1, the rest read past it
-  uint32_t l1_hot_bytes = 160u << 10;
+  uint32_t l1_hot_bytes = 0xffffffffu;
+  // CC and SSSP: a dense call (by the reference's switch) whose active
+  // out-edges are below nadj / dense_push_div runs the push kernels over the
+  // frontier instead of pulling every in-list (0: always pull; 4 measured
+  // best for SSSP on R-MAT 25, neutral for CC on R-MAT 26)
+  uint32_t dense_push_div = 4;
+  // PageRank's iterations captured as one CUDA graph, replayed while the key
+  // (arguments, buffers, events) is unchanged
+  cudaGraphExec_t pr_exec[2] = {nullptr, nullptr};  // float, double
+  PrGraphKey pr_key[2];
 };
 
 namespace gg {
@@ -224,6 +245,11 @@ struct Trace {
   std::vector<int> ev_call;
   std::vector<cudaEvent_t> ev;
   int nvtx_depth = 0;
+  // replay of a captured run: kbegin / kend name the events the graph
+  // records instead of recording them
+  bool replay = false;
+  bool capturing = false;  // the graph's stream is being captured
+  int record(cudaEvent_t e);
   Trace(gg_run_stats *s, gg_graph *gr, const char *run = nullptr) : st(s), g(gr) {
     if (run) {
       nvtxRangePushA(run);
@@ -278,8 +304,10 @@ struct Trace {
     if (i >= 0 && i < st->trace_capacity && st->activated) st->activated[i] = activated;
   }
   bool timing() const { return st && st->call_ms && st->calls >= 1 && st->calls - 1 < st->trace_capacity; }
+  int timing_requested() const { return st && st->call_ms ? 1 + st->trace_capacity : 0; }
   int kbegin();
   int kend();
+  int reserve_events(size_t n);  // before a capture: no event is created inside it
   int collect();  // after the stream has been synchronised
 };
 
@@ -347,7 +375,7 @@ __device__ __forceinline__ double ld_once(const double *p) {
 // was written by an earlier kernel, so the read-only path is safe.
 template <typename T>
 __device__ __forceinline__ T ld_gather(const T *a, uint32_t u, uint32_t hot) {
-  return u < hot ? __ldg(a + u) : ld_once(a + u);
+  return u < hot ? a[u] : ld_once(a + u);
 }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 

@@ -854,6 +854,8 @@ struct Launch {
   unsigned heavy_grid(const Dir &d) const {
     return grid_for((size_t)d.nchunks * 32, PULL_THREADS, g->num_sms, 8);
   }
+  // Kernels one reduction pull launches.
+  static int pull_launches(const Dir &d) { return d.nbig ? 3 : 1; }
   // All bins of one dense call, in order: light, medium, heavy chunks, heavy finish.
   template <class Op>
   int pull(const Dir &d, const Op &op, const ActOut &act, Counters *ctr) {

@@ -103,18 +103,34 @@ int counters_reset(gg_graph *g) {
 
 int counters_read(gg_graph *g, Counters *out) { return read_small(g, out, g->ws.ctr, sizeof(Counters)); }
 
-int Trace::kbegin() {
-  if (!timing()) return GG_OK;
-  size_t need = ev.size() + 2;
-  while (g->evpool.size() < need) {
+int Trace::reserve_events(size_t n) {
+  if (!st || !st->call_ms) return GG_OK;
+  while (g->evpool.size() < ev.size() + n) {
     cudaEvent_t e;
     GG_CUDA(cudaEventCreate(&e));
     g->evpool.push_back(e);
   }
+  return GG_OK;
+}
+
+// Inside a stream capture the record is made an external event node, which
+// records the event when the graph runs (so that it can be timed); the flag
+// is refused outside a capture.
+int Trace::record(cudaEvent_t e) {
+  if (capturing)
+    GG_CUDA(cudaEventRecordWithFlags(e, g->stream, cudaEventRecordExternal));
+  else
+    GG_CUDA(cudaEventRecord(e, g->stream));
+  return GG_OK;
+}
+
+int Trace::kbegin() {
+  if (!timing()) return GG_OK;
+  GG_TRY(reserve_events(2));
   cudaEvent_t e0 = g->evpool[ev.size()];
   ev.push_back(e0);
   ev_call.push_back(st->calls - 1);
-  GG_CUDA(cudaEventRecord(e0, g->stream));
+  if (!replay) GG_TRY(record(e0));
   return GG_OK;
 }
 
@@ -122,7 +138,7 @@ int Trace::kend() {
   if (!timing() || ev.size() % 2 == 0) return GG_OK;
   cudaEvent_t e1 = g->evpool[ev.size()];
   ev.push_back(e1);
-  GG_CUDA(cudaEventRecord(e1, g->stream));
+  if (!replay) GG_TRY(record(e1));
   return GG_OK;
 }
 
@@ -796,6 +812,10 @@ void graph_destroy(gg_graph *g) {
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
   pools_destroy(g);
+  for (cudaGraphExec_t &x : g->pr_exec) {
+    if (x) cudaGraphExecDestroy(x);
+    x = nullptr;
+  }
   pr_layout_free(g);
   bool alias = g->in.nbr == g->out.nbr;
   free_dir(&g->out, g->adj_host);

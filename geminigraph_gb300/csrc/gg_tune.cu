@@ -5,9 +5,12 @@
 // graph itself: every candidate rebuilds the bins and times, with CUDA
 // events, the objective's workloads: four float PageRank iterations (light
 // and chunked pulls), one BFS from the vertex of largest out-degree (push,
-// pull, small runs) and one 64-root batched BFS (and SSSP on a weighted
-// graph); the
-// fastest is kept and recorded in a cache file keyed by a fingerprint of the
+// pull, small runs), one 64-root batched BFS (and SSSP on a weighted
+// graph), one SSSP from that vertex, one CC; the
+// fastest is kept.  With the PageRank objective the pulls' L1 policy is then
+// chosen the same way: every gather cached in L1, or only the hottest
+// sources' (measured faster where the state array is small enough to stay in
+// L2).  The choice is recorded in a cache file keyed by a fingerprint of the
 // graph, so the next load of the same graph skips the search.
 #include <stdio.h>
 #include <stdlib.h>
@@ -52,7 +55,7 @@ static std::string cache_file(const char *dir) {
   } else {
     d = "/tmp/geminigraph_gb300";
   }
-  return d + "/bins_v2.txt";
+  return d + "/bins_v3.txt";
 }
 
 static void mkdirs(const std::string &path) {
@@ -79,8 +82,14 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     set_error("null graph");
     return GG_ERR_INVALID;
   }
-  if (objective == 0 || (objective & ~(uint32_t)(GG_TUNE_PAGERANK | GG_TUNE_BFS | GG_TUNE_BATCHED))) {
-    set_error("objective must be a non-empty mask of GG_TUNE_PAGERANK, GG_TUNE_BFS and GG_TUNE_BATCHED");
+  const uint32_t all = GG_TUNE_PAGERANK | GG_TUNE_BFS | GG_TUNE_BATCHED | GG_TUNE_SSSP | GG_TUNE_CC;
+  if (objective == 0 || (objective & ~all)) {
+    set_error("objective must be a non-empty mask of GG_TUNE_PAGERANK, GG_TUNE_BFS, GG_TUNE_BATCHED, GG_TUNE_SSSP "
+              "and GG_TUNE_CC");
+    return GG_ERR_INVALID;
+  }
+  if (((objective & GG_TUNE_SSSP) && !g->weighted) || ((objective & GG_TUNE_CC) && !g->symmetric)) {
+    set_error("the SSSP objective needs a weighted graph, the CC objective a symmetric one");
     return GG_ERR_INVALID;
   }
   GG_CUDA(cudaSetDevice(g->device));
@@ -114,13 +123,14 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   const std::string file = cache_file(cache_dir);
   if (FILE *f = fopen(file.c_str(), "r")) {
     char k[160];
-    unsigned light, chunk, vec;
+    unsigned light, chunk, vec, l1;
     double ms;
-    while (fscanf(f, "%159s %u %u %u %lf", k, &light, &chunk, &vec, &ms) == 5) {
+    while (fscanf(f, "%159s %u %u %u %u %lf", k, &light, &chunk, &vec, &l1, &ms) == 6) {
       if (std::string(k) == key) {
         r.light_deg = light;
         r.pull_chunk = chunk;
         r.pull_vector = vec;
+        r.l1_hot_bytes = l1;
         r.best_ms = ms;
         r.from_cache = 1;
       }
@@ -128,6 +138,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     fclose(f);
     if (r.from_cache) {
       GG_TRY(rebuild_bins(g, r.light_deg, r.pull_chunk, r.pull_vector));
+      g->l1_hot_bytes = r.l1_hot_bytes;
       if (out) *out = r;
       return GG_OK;
     }
@@ -160,6 +171,14 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
       GG_TRY(gg_bfs(g, root, nullptr, &st));
       t += st.device_ms;
     }
+    if (objective & GG_TUNE_SSSP) {
+      GG_TRY(gg_sssp(g, root, nullptr, &st));
+      t += st.device_ms;
+    }
+    if (objective & GG_TUNE_CC) {
+      GG_TRY(gg_cc(g, nullptr, &st));
+      t += st.device_ms;
+    }
     if (objective & GG_TUNE_BATCHED) {
       GG_TRY(gg_bfs_batched(g, roots.data(), (int)roots.size(), nullptr, nullptr, nullptr, nullptr, &st));
       t += st.device_ms;
@@ -190,6 +209,22 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
         }
       }
   GG_TRY(rebuild_bins(g, bl, bc, bv));
+  uint32_t bh = 0xffffffffu;
+  g->l1_hot_bytes = bh;
+  if (objective & GG_TUNE_PAGERANK) {
+    const uint32_t hot = 160u << 10;
+    g->l1_hot_bytes = hot;
+    double ms0, ms1;
+    GG_TRY(measure(&ms0));  // warm
+    GG_TRY(measure(&ms1));
+    r.candidates += 1;
+    if (ms1 < best) {
+      best = ms1;
+      bh = hot;
+    }
+    g->l1_hot_bytes = bh;
+  }
+  r.l1_hot_bytes = bh;
   r.light_deg = bl;
   r.pull_chunk = bc;
   r.pull_vector = bv;
@@ -197,7 +232,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   r.default_ms = def;
   mkdirs(file);
   if (FILE *f = fopen(file.c_str(), "a")) {
-    fprintf(f, "%s %u %u %u %.6f\n", key, bl, bc, bv, best);
+    fprintf(f, "%s %u %u %u %u %.6f\n", key, bl, bc, bv, bh, best);
     fclose(f);
   }
   if (out) *out = r;

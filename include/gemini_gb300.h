@@ -339,6 +339,8 @@ typedef struct {
   double default_ms;     /* the same with the defaults (32, 256, 1) */
   int32_t candidates;    /* candidates timed (0 when read from the cache) */
   int32_t from_cache;
+  uint32_t l1_hot_bytes; /* the pulls' L1 policy kept (gg_graph_set_l1_hot; PageRank
+                            objective: every gather cached, or the hottest 160 KiB) */
 } gg_tune_result;
 
 int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint32_t pull_vector);
@@ -346,6 +348,8 @@ int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint
 #define GG_TUNE_PAGERANK 1u
 #define GG_TUNE_BFS 2u
 #define GG_TUNE_BATCHED 4u
+#define GG_TUNE_SSSP 8u    /* one SSSP from the vertex of largest out-degree (weighted graphs) */
+#define GG_TUNE_CC 16u     /* one CC (symmetric graphs) */
 int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_result *out);
 
 /* PageRank's adjacency layout (no reference counterpart; the reference pulls
@@ -369,8 +373,20 @@ int gg_graph_set_pr_layout(gg_graph *g, int hot_sources);
  * ones -- is cached in each SM's L1, and every other gather is read past L1 so
  * that it does not evict them.  0 reads every gather past L1; a value at least
  * the whole state array caches every gather (the plain layout always does).
- * Results do not depend on it.  Default 163840 (160 KiB). */
+ * Results do not depend on it.  Default: every gather cached (measured
+ * fastest on R-MAT 24 and 26, where the other gathers reuse L1 lines too). */
 int gg_graph_set_l1_hot(gg_graph *g, uint32_t l1_bytes);
+
+/* Kernel choice for the dense calls of gg_cc and gg_sssp (no reference
+ * counterpart; the reference's dense mode pulls every in-list,
+ * core/graph.hpp:1664-1855).  A call that the reference's switch makes dense
+ * runs as a push over the frontier when its active out-edges are below
+ * adjacency entries / divisor; 0 always pulls.  A source that is not active
+ * cannot lower a neighbour's label or distance, so both forms give the same
+ * values, the same activated set and the same per-call trace (which records
+ * the reference's mode).  Default 4 (measured on R-MAT 25 SSSP: 131 -> 145
+ * GTEPS; CC on R-MAT 26 unchanged). */
+int gg_graph_set_dense_push(gg_graph *g, uint32_t divisor);
 
 /* ---- engine primitives ---- */
 

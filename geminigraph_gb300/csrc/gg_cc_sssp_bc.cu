@@ -86,6 +86,8 @@ struct SsspPull {
   __device__ __forceinline__ float gather(const Dir &d, unsigned long long k, uint32_t u) const {
     return __fadd_rn(ld_gather(cur, u, hot), d.w[k]);
   }
+  // the same candidate with the weight read by the kernel
+  __device__ __forceinline__ float gather_w(uint32_t u, float w) const { return __fadd_rn(ld_gather(cur, u, hot), w); }
   __device__ __forceinline__ float combine(float a, float b) const { return b < a ? b : a; }
   __device__ __forceinline__ float warp_combine(float x) const { return warp_min(x); }
   __device__ __forceinline__ bool finish(uint32_t v, float m, uint32_t, Tally &) const {

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "gg_common.cuh"
 #include "gg_scan.cuh"
@@ -30,6 +31,14 @@
 namespace gg {
 
 constexpr uint32_t NONE32 = 0xffffffffu;
+
+// Ops whose gather adds an edge weight (SSSP) may take the weight from the
+// kernel (gather_w): the chunk kernel reads weights coalesced and past L1,
+// as it reads neighbour ids, so that L1 keeps the gathered state.
+template <class Op, class = void>
+struct has_gather_w : std::false_type {};
+template <class Op>
+struct has_gather_w<Op, std::void_t<decltype(&Op::gather_w)>> : std::true_type {};
 constexpr int PUSH_THREADS = 256;
 constexpr int PUSH_TILE = 1024;              // edges per block iteration of push_lb
 constexpr int PUSH_STAGE = PUSH_TILE + 1;    // queue entries a tile spans when each has >= 1 edge
@@ -241,32 +250,48 @@ __global__ void __launch_bounds__(PULL_THREADS)
     Acc part = op.identity_coop();
     if (op.want(v)) {
       Acc vals[PER_LANE];
+      constexpr bool WT = has_gather_w<Op>::value;
       if constexpr (VEC) {
-        uint4 w[WIN];
+        uint4 w[WIN], wt[WT ? WIN : 1];
 #pragma unroll
         for (int i = 0; i < WIN; i++) {
           const unsigned long long p = lo + 4 * (lane + 32 * i);
-          w[i] = p < e && p + 4 > b ? ld_once_v4(d.nbr + p) : make_uint4(0, 0, 0, 0);
+          const bool in = p < e && p + 4 > b;
+          w[i] = in ? ld_once_v4(d.nbr + p) : make_uint4(0, 0, 0, 0);
+          if constexpr (WT)
+            wt[i] = in ? ld_once_v4(reinterpret_cast<const uint32_t *>(d.w) + p) : make_uint4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int i = 0; i < WIN; i++) {
           const unsigned long long p = lo + 4 * (lane + 32 * i);
           const uint32_t u[4] = {w[i].x, w[i].y, w[i].z, w[i].w};
 #pragma unroll
-          for (int j = 0; j < 4; j++)
-            vals[4 * i + j] = p + j >= b && p + j < e ? op.gather(d, p + j, u[j]) : op.identity_coop();
+          for (int j = 0; j < 4; j++) {
+            const bool in = p + j >= b && p + j < e;
+            if constexpr (WT) {
+              const uint32_t wb[4] = {wt[i].x, wt[i].y, wt[i].z, wt[i].w};
+              vals[4 * i + j] = in ? op.gather_w(u[j], __uint_as_float(wb[j])) : op.identity_coop();
+            } else {
+              vals[4 * i + j] = in ? op.gather(d, p + j, u[j]) : op.identity_coop();
+            }
+          }
         }
       } else {
         uint32_t u[PER_LANE];
+        float wt[WT ? PER_LANE : 1];
 #pragma unroll
         for (int j = 0; j < PER_LANE; j++) {
           const unsigned long long k = b + lane + 32 * j;
           u[j] = k < e ? ld_once(d.nbr + k) : 0u;
+          if constexpr (WT) wt[j] = k < e ? ld_once(d.w + k) : 0.0f;
         }
 #pragma unroll
         for (int j = 0; j < PER_LANE; j++) {
           const unsigned long long k = b + lane + 32 * j;
-          vals[j] = k < e ? op.gather(d, k, u[j]) : op.identity_coop();
+          if constexpr (WT)
+            vals[j] = k < e ? op.gather_w(u[j], wt[j]) : op.identity_coop();
+          else
+            vals[j] = k < e ? op.gather(d, k, u[j]) : op.identity_coop();
         }
       }
 #pragma unroll

@@ -452,11 +452,15 @@ int build_plan(gg_graph *g, uint64_t E, bool rec_on_device, const gg_build_optio
   // offsets scan; then a group buffer of G entries (key + value) and one
   // range's sort buffer and digit counts, ranges of at most G/4 entries.
   // Greedy ranges of at most cap entries number at most 2n/cap + 1, so the
-  // count table is sized for that many (at least 64), refined until it fits.
+  // count table is sized for that many (at least 64), refined until the
+  // table and cap agree: every pass that grows the table recomputes cap, and
+  // the table only grows, up to OC_MAX_PARTS, so the loop ends.  (A list
+  // longer than cap is still a range of its own, sorted in a buffer of its
+  // length, which can exceed the budget.)
   const uint64_t tiles = (n + OC_TILE - 1) / OC_TILE;
   const uint64_t kv = 8 + (g->weighted ? 4 : 0);
   uint64_t ranges = 64;
-  for (int it = 0; it < 4; it++) {
+  for (;;) {
     const uint64_t fixed = (uint64_t)g->V * 8 + tiles * 8 * ranges + (64ull << 20);
     const uint64_t avail = budget > fixed ? budget - fixed : 0;
     *gcap = avail * 4 / (4 * kv + kv + 1);

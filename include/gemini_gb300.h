@@ -403,12 +403,15 @@ int gg_active_edges(gg_graph *g, const uint64_t *active_bitmap, uint64_t *active
  * device memory the caller provides: d_bitmap (vertices/64+1 64-bit words, the
  * reference's bitmap layout), d_degree (vertices out-degrees), d_active_edges
  * (one uint64 that receives the sum).  stream is a cudaStream_t, or NULL for
- * the default stream; the call returns once that stream has finished.
+ * the default stream; the call returns once that stream has finished.  It
+ * runs on the calling thread's current device.
  * It allocates nothing: its only scratch is a fixed 32 KiB device array inside
  * the library (one partial sum per 65,536 vertices), so it accepts at most
  * GG_NOALLOC_MAX_VERTICES vertices and returns GG_ERR_LIMIT beyond.  The first
- * call on a device looks up that array's device address (cudaGetSymbolAddress):
- * make that first call before any stream capture.  All calls share the array,
+ * call on a device looks up that array's device address (cudaGetSymbolAddress)
+ * and keeps it for the life of the process: make that first call before any
+ * stream capture, and do not reset the device (cudaDeviceReset) after it.
+ * All calls share the array,
  * which keeps the last call's partial sums; calls that overlap on the GPU race. */
 #define GG_NOALLOC_MAX_VERTICES 268435456u
 int gg_active_edges_noalloc(const uint64_t *d_bitmap, const uint32_t *d_degree, uint32_t vertices,

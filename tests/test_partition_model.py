@@ -127,3 +127,38 @@ def test_partitioned_model_equals_in_core(V, E, weighted, mode, force):
     off2, nbr2, w2, nparts, ngroups = partitioned(rec, V, mode, force)
     assert np.array_equal(off, off2) and np.array_equal(nbr, nbr2) and np.array_equal(w, w2)
     assert 1 <= ngroups <= nparts <= MAX_PARTS
+
+
+def plan(V, n, weighted, budget, tile=4096, max_parts=1024):
+    """build_plan's sizing arithmetic (gg_partition.cu): the (range, tile)
+    count table sized for `ranges`, a group buffer of gcap entries, one
+    range's sort buffer and digit counts of cap = gcap / 4 entries."""
+    tiles = (n + tile - 1) // tile
+    kv = 8 + (4 if weighted else 0)
+    ranges = 64
+    while True:
+        fixed = V * 8 + tiles * 8 * ranges + (64 << 20)
+        avail = budget - fixed if budget > fixed else 0
+        gcap = avail * 4 // (4 * kv + kv + 1)
+        cap = gcap // 4
+        if cap == 0:
+            return cap, gcap, ranges, fixed
+        need = min(2 * n // cap + 1, max_parts)
+        if need <= ranges:
+            return cap, gcap, ranges, fixed
+        ranges = need
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+@pytest.mark.parametrize("V,n", [(1 << 20, 1 << 24), (1 << 24, 1 << 28), (1 << 26, 1 << 30), (1 << 26, 1 << 31)])
+@pytest.mark.parametrize("budget_mb", [200, 300, 600, 1000, 4000, 16000])
+def test_build_plan_stays_within_budget(V, n, weighted, budget_mb):
+    budget = budget_mb << 20
+    cap, gcap, ranges, fixed = plan(V, n, weighted, budget)
+    if cap < (1 << 16) and cap < n:
+        return                                        # refused: GG_ERR_NOMEM
+    kv = 8 + (4 if weighted else 0)
+    planned = fixed + gcap * kv + cap * kv + cap      # group buffer, sort buffer, digit counts
+    assert planned <= budget
+    # the count table holds every range that cap implies (capped at the kernel's maximum)
+    assert min(2 * n // cap + 1, 1024) <= ranges

@@ -735,6 +735,16 @@ def gpu_arm_batched(args, dist):
     }
     if bfs:
         line["lane_gteps"] = round(dist.sum(edges) / t_max / 1e9, 2)
+    if bc and first is not None:
+        # level storage of the first batch: a 12-byte list entry per (vertex,
+        # level) pair occurring in some lane plus two dense u64 mask arrays,
+        # against one u64 mask per vertex per level
+        rows = first.rows()
+        fwd = rows[:len(rows) // 2]
+        pairs = len(set(batches[args.warmup])) + sum(r[2] for r in fwd)
+        line["level_storage"] = {"levels": len(fwd), "pairs": pairs,
+                                 "bytes_per_vertex": round((12 * pairs + 16 * V) / V, 2),
+                                 "per_level_masks_bytes_per_vertex": 8 * len(fwd)}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     g.close()

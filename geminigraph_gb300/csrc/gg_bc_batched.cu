@@ -5,8 +5,13 @@
 // Layout (vertex-major, lane l of vertex v at v * 64 + l):
 //   np   double  path counts; 1 / np is the reference's inv_num_paths
 //   dep  double  dependencies
-//   lev  one u64 lane mask per vertex per level (the reference's per-level
-//        VertexSubsets, bc.cpp:34-35, one bit per lane)
+//   levels  per level, the compacted list of the vertices on it in some lane
+//           with their lane masks (uint32 id + u64 mask): the memory trade of
+//           the reference's compute_compact (bc.cpp:198-404, a level array
+//           instead of one bitmap per level, bc.cpp:34-35).  12 B per
+//           (vertex, level) pair that occurs in some lane, instead of 8 B per
+//           vertex per level; two dense u64 mask arrays are rebuilt from the
+//           lists for the level at hand and the next one.
 //   visit u64    lanes that have reached the vertex
 // Forward (bc.cpp:48-111), per level and for all lanes at once: the sparse /
 // dense switch on the union frontier's out-degree sum (core/graph.hpp:1509);
@@ -52,22 +57,33 @@ __global__ void bcb_init(const uint32_t *roots, int n, u64 *visit, u64 *front, d
   }
 }
 
-// Out-degree sum and count of the frontier's vertices (any lane).
-__global__ void bcb_frontier_stats(const u64 *__restrict__ front, const uint32_t *__restrict__ out_deg, uint32_t V,
-                                   Counters *ctr) {
-  Tally t;
-  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
-    if (front[v]) {
-      t.edges += out_deg[v];
-      t.activated += 1;
+// The level list of a dense mask array: (v, m[v]) for m[v] != 0, in vertex order.
+__global__ void bcb_compact(const u64 *__restrict__ m, uint32_t V, const uint32_t *__restrict__ pos,
+                            uint32_t *__restrict__ qv, u64 *__restrict__ qm) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x) {
+    const u64 x = m[v];
+    if (x) {
+      qv[pos[v]] = (uint32_t)v;
+      qm[pos[v]] = x;
     }
-  t.flush(ctr);
+  }
 }
 
-__global__ void bcb_compact(const u64 *__restrict__ m, uint32_t V, const uint32_t *__restrict__ pos,
-                            uint32_t *__restrict__ q) {
-  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
-    if (m[v]) q[pos[v]] = (uint32_t)v;
+// dense[qv[i]] = qm[i], or 0 for every listed vertex when qm is null.
+__global__ void bcb_scatter(const uint32_t *__restrict__ qv, const u64 *__restrict__ qm, uint32_t n, u64 *dense) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dense[qv[i]] = qm ? qm[i] : 0ull;
+}
+
+// Out-degree sum of a level list (the switch's active_edges).
+__global__ void bcb_list_degrees(const uint32_t *__restrict__ qv, uint32_t n, const uint32_t *__restrict__ out_deg,
+                                 Counters *ctr) {
+  Tally t;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    t.edges += out_deg[qv[i]];
+    t.activated += 1;
+  }
+  t.flush(ctr);
 }
 
 // Sparse level: every out-edge of the queued frontier, edge-balanced (edge e
@@ -355,14 +371,13 @@ static int bc_batched_run(gg_graph *g, const uint32_t *roots, int n, double *dep
   GG_CUDA(cudaSetDevice(g->device));
   cudaStream_t s = g->stream;
   const size_t lanes_bytes = sizeof(double) * (size_t)V * BCB_LANES;
-  DevBuf np_b, dep_b, visit_b, alive_b, roots_b, part_b, out_b, q_b, qpos_b, prefix_b, scan_b, scan64_b, ctr_b;
+  DevBuf np_b, dep_b, visit_b, alive_b, roots_b, part_b, out_b, qpos_b, prefix_b, scan_b, scan64_b, ctr_b;
   GG_CUDA(cudaMalloc(&np_b.p, lanes_bytes));
   GG_CUDA(cudaMalloc(&dep_b.p, lanes_bytes));
   GG_CUDA(cudaMalloc(&visit_b.p, sizeof(u64) * V));
   GG_CUDA(cudaMalloc(&alive_b.p, sizeof(u64)));
   GG_CUDA(cudaMalloc(&roots_b.p, sizeof(uint32_t) * BCB_LANES));
   GG_CUDA(cudaMalloc(&ctr_b.p, sizeof(Counters)));
-  GG_CUDA(cudaMalloc(&q_b.p, sizeof(uint32_t) * ((size_t)V + 1)));
   GG_CUDA(cudaMalloc(&qpos_b.p, sizeof(uint32_t) * ((size_t)V + 1)));
   GG_CUDA(cudaMalloc(&prefix_b.p, sizeof(u64) * ((size_t)V + 1)));
   GG_CUDA(cudaMalloc(&scan_b.p, sizeof(uint32_t) * scan_scratch_elems((size_t)V + 1)));
@@ -372,55 +387,79 @@ static int bc_batched_run(gg_graph *g, const uint32_t *roots, int n, double *dep
   double *np = (double *)np_b.p, *dep = (double *)dep_b.p, *part = (double *)part_b.p;
   u64 *visit = (u64 *)visit_b.p, *alive_d = (u64 *)alive_b.p;
   Counters *ctr = (Counters *)ctr_b.p;
-  uint32_t *q = (uint32_t *)q_b.p, *qpos = (uint32_t *)qpos_b.p;
+  uint32_t *qpos = (uint32_t *)qpos_b.p;
   u64 *prefix = (u64 *)prefix_b.p;
-  std::vector<DevBuf> levels;  // one lane mask per vertex per level
-  auto new_level = [&](u64 **out) -> int {
+  // level lists (vertex ids, lane masks, count) and the two dense mask arrays
+  struct Level {
+    DevBuf v, m;
+    uint32_t n = 0;
+  };
+  std::vector<Level> levels;
+  DevBuf dense_b[2];
+  for (DevBuf &b : dense_b) GG_CUDA(cudaMalloc(&b.p, sizeof(u64) * V));
+  u64 *dense[2] = {(u64 *)dense_b[0].p, (u64 *)dense_b[1].p};
+  auto new_level = [&](uint32_t count) -> int {
     levels.emplace_back();
-    GG_CUDA(cudaMalloc(&levels.back().p, sizeof(u64) * V));
-    GG_CUDA(cudaMemsetAsync(levels.back().p, 0, sizeof(u64) * V, s));
-    *out = (u64 *)levels.back().p;
+    Level &l = levels.back();
+    l.n = count;
+    GG_CUDA(cudaMalloc(&l.v.p, sizeof(uint32_t) * (count ? count : 1)));
+    GG_CUDA(cudaMalloc(&l.m.p, sizeof(u64) * (count ? count : 1)));
     return GG_OK;
   };
+  auto lv = [&](int L) { return (const uint32_t *)levels[L].v.p; };
+  auto lm = [&](int L) { return (const u64 *)levels[L].m.p; };
   Trace tr(st, g, "gg_bc_batched");
   int launches = 0;
+  // level 0: the distinct roots and their lanes
+  std::vector<uint32_t> r0;
+  std::vector<u64> m0;
+  for (int i = 0; i < n; i++) {
+    size_t j = 0;
+    while (j < r0.size() && r0[j] != roots[i]) j++;
+    if (j == r0.size()) {
+      r0.push_back(roots[i]);
+      m0.push_back(0);
+    }
+    m0[j] |= 1ull << i;
+  }
+  GG_TRY(new_level((uint32_t)r0.size()));
+  GG_CUDA(cudaMemcpyAsync(levels[0].v.p, r0.data(), sizeof(uint32_t) * r0.size(), cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaMemcpyAsync(levels[0].m.p, m0.data(), sizeof(u64) * m0.size(), cudaMemcpyHostToDevice, s));
   GG_CUDA(cudaMemcpyAsync(roots_b.p, roots, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
   GG_TRY(timed_begin(g));
   GG_CUDA(cudaMemsetAsync(np, 0, lanes_bytes, s));
   GG_CUDA(cudaMemsetAsync(dep, 0, lanes_bytes, s));
   GG_CUDA(cudaMemsetAsync(visit, 0, sizeof(u64) * V, s));
-  u64 *front;
-  GG_TRY(new_level(&front));
+  GG_CUDA(cudaMemsetAsync(dense[0], 0, sizeof(u64) * V, s));
+  GG_CUDA(cudaMemsetAsync(dense[1], 0, sizeof(u64) * V, s));
+  int cur = 0;
+  u64 *front = dense[cur];
   bcb_init<<<1, BCB_LANES, 0, s>>>((const uint32_t *)roots_b.p, n, visit, front, np);
   launches += 1;
   const u64 all = n == 64 ? ~0ull : ((1ull << n) - 1);
   u64 alive = all;
   const unsigned vg = grid_for(V, 256, g->num_sms, 8);
   // ---- forward
-  for (;;) {
+  for (int L = 0;; L++) {
     Counters hc;
+    const uint32_t nL = levels[L].n;
     GG_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), s));
-    bcb_frontier_stats<<<vg, 256, 0, s>>>(front, g->out.deg, V, ctr);
+    bcb_list_degrees<<<grid_for(nL ? nL : 1, 256, g->num_sms, 8), 256, 0, s>>>(lv(L), nL, g->out.deg, ctr);
     GG_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     GG_CUDA(cudaStreamSynchronize(s));
     launches += 1;
     const u64 ae = hc.edges;
     const bool sparse = ae < g->E / 20;
     tr.add(sparse ? 0 : 1, ae, 0);
-    u64 *next;
-    GG_TRY(new_level(&next));
+    u64 *next = dense[cur ^ 1];
     if (sparse) {
       if (ae) {
-        GG_CUDA((exclusive_scan<uint32_t, NonzeroU64>(NonzeroU64{front}, V, qpos, (uint32_t *)scan_b.p, s,
-                                                      &launches)));
-        bcb_compact<<<vg, 256, 0, s>>>(front, V, qpos, q);
-        uint32_t nq = 0;
-        GG_CUDA(cudaMemcpyAsync(&nq, qpos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        GG_CUDA(cudaStreamSynchronize(s));
-        GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q, g->out.deg}, nq, prefix,
+        // the level list is the frontier queue
+        GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{lv(L), g->out.deg}, nL, prefix,
                                                                     (u64 *)scan64_b.p, s, &launches)));
-        bcb_push<<<grid_for(ae, 256, g->num_sms, 16), 256, 0, s>>>(g->out, q, prefix, nq, front, visit, next, np);
-        launches += 2;
+        bcb_push<<<grid_for(ae, 256, g->num_sms, 16), 256, 0, s>>>(g->out, lv(L), prefix, nL, front, visit, next,
+                                                                   np);
+        launches += 1;
       }
     } else {
       bcb_pull_light<<<grid_for((size_t)V, 256, g->num_sms, 8), 256, 0, s>>>(g->in, V, alive, front, visit, next,
@@ -441,28 +480,51 @@ static int bc_batched_run(gg_graph *g, const uint32_t *roots, int n, double *dep
     GG_CUDA(cudaMemcpyAsync(&alive, alive_d, sizeof(u64), cudaMemcpyDeviceToHost, s));
     GG_CUDA(cudaStreamSynchronize(s));
     tr.set_activated(hc.activated);
+    // the next level's list, then this level's dense masks cleared for reuse
+    if (hc.activated) {
+      GG_TRY(new_level(hc.activated));
+      GG_CUDA((exclusive_scan<uint32_t, NonzeroU64>(NonzeroU64{next}, V, qpos, (uint32_t *)scan_b.p, s,
+                                                    &launches)));
+      bcb_compact<<<vg, 256, 0, s>>>(next, V, qpos, (uint32_t *)levels[L + 1].v.p, (u64 *)levels[L + 1].m.p);
+      launches += 1;
+    }
+    bcb_scatter<<<grid_for(nL ? nL : 1, 256, g->num_sms, 8), 256, 0, s>>>(lv(L), nullptr, nL, front);
+    launches += 1;
+    GG_CUDA(cudaGetLastError());
+    cur ^= 1;
     front = next;
     if (!alive) break;
   }
-  // levels[0 .. D-1] hold vertices, levels[D] is empty
-  const int D = (int)levels.size() - 1;
-  // ---- backward, deepest level first
+  // both dense arrays are zero here: the last `next` had no lane, the other was cleared
+  const int D = (int)levels.size();
+  // ---- backward, deepest level first; cur / nxt are the dense masks of
+  // levels L and L + 1, rebuilt from the lists
   const Dir &od = g->out;
   for (int L = D - 1; L >= 0; L--) {
-    const u64 *cur = (const u64 *)levels[L].p;
-    const u64 *nxt = L + 1 < D ? (const u64 *)levels[L + 1].p : nullptr;
+    u64 *curm = dense[L & 1];
+    u64 *nxtm = dense[(L + 1) & 1];
+    const uint32_t nL = levels[L].n;
+    bcb_scatter<<<grid_for(nL ? nL : 1, 256, g->num_sms, 8), 256, 0, s>>>(lv(L), lm(L), nL, curm);
+    launches += 1;
+    const u64 *nxt = L + 1 < D ? nxtm : nullptr;
     tr.add(1, 0, 0);
-    bcb_back_light<<<grid_for((size_t)V, 256, g->num_sms, 8), 256, 0, s>>>(od, V, cur, nxt, dep, np);
+    bcb_back_light<<<grid_for((size_t)V, 256, g->num_sms, 8), 256, 0, s>>>(od, V, curm, nxt, dep, np);
     launches += 1;
     if (od.nbig) {
       if (nxt) {
-        bcb_back_chunks<<<grid_for((size_t)od.nbigchunks * 32, 256, g->num_sms, 8), 256, 0, s>>>(od, cur, nxt, dep,
+        bcb_back_chunks<<<grid_for((size_t)od.nbigchunks * 32, 256, g->num_sms, 8), 256, 0, s>>>(od, curm, nxt, dep,
                                                                                                  part);
       } else {
         GG_CUDA(cudaMemsetAsync(part, 0, sizeof(double) * BCB_LANES * od.nbigchunks, s));
       }
-      bcb_back_finish<<<grid_for((size_t)od.nbig * 32, 256, g->num_sms, 8), 256, 0, s>>>(od, cur, part, dep, np);
+      bcb_back_finish<<<grid_for((size_t)od.nbig * 32, 256, g->num_sms, 8), 256, 0, s>>>(od, curm, part, dep, np);
       launches += 2;
+    }
+    if (L + 1 < D) {
+      // level L + 1's masks are no longer needed: clear them for level L - 1
+      bcb_scatter<<<grid_for(levels[L + 1].n, 256, g->num_sms, 8), 256, 0, s>>>(lv(L + 1), nullptr, levels[L + 1].n,
+                                                                                nxtm);
+      launches += 1;
     }
     GG_CUDA(cudaGetLastError());
   }

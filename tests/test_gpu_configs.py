@@ -169,13 +169,24 @@ def test_sssp_batched_64_rmat20_against_oracle():
 def test_bc_batched_64_rmat20_against_oracle():
     V, g, og, deg = graph_pair(oracle.RMAT, 20)
     roots = batch_roots(deg, 3003)
-    dep, inv, reached, _ = gg.bc_batched(g, roots, outputs=True)
+    dep, inv, reached, st = gg.bc_batched(g, roots, outputs=True)
     outs = pmap(lambda r: og.bc(r)[:2], roots)
     for i, (r, (odep, oinv)) in enumerate(zip(roots, outs)):
         assert np.array_equal(np.isnan(dep[i]), np.isnan(odep)), f"lane {i} root {r}"
         assert np.array_equal(inv[i], oinv), f"lane {i} root {r}"
         ok = ~np.isnan(odep)
         assert rel_l1(dep[i][ok], odep[ok]) < BC_TOL, f"lane {i} root {r}"
+    # level storage: one list entry per (vertex, level) pair that occurs in
+    # some lane -- the level sizes in the trace (forward calls first, then one
+    # backward call per level) against the oracle's per-lane levels
+    rows = st.rows()
+    forward = rows[:len(rows) // 2]
+    pairs = len(set(roots)) + sum(r[2] for r in forward)
+    lv = np.stack([oracle.tree_levels(og.bfs(r)[0], r) for r in roots])
+    lv = np.sort(lv, axis=0)
+    distinct = (lv[0] >= 0).astype(np.int64) + ((lv[1:] != lv[:-1]) & (lv[1:] >= 0)).sum(axis=0)
+    assert pairs == int(distinct.sum())
+    assert len(forward) == int(lv.max()) + 1
 
 
 def test_bfs_grid1024():

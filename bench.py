@@ -826,41 +826,21 @@ def pct(xs, q):
     return xs[min(len(xs) - 1, int(round(q / 100.0 * (len(xs) - 1))))] if xs else None
 
 
-def gpu_arm_serve(args, dist):
-    """One step = one query of the stream.  value = completed queries / the
-    span from the first arrival to the last completion; plain = the first
-    args.plain queries run one at a time through gg_bfs / gg_sssp with the same
-    arrival times (FIFO, device time as service time)."""
-    import threading
+def fifo_replay(arrivals, service):
+    """One-at-a-time FIFO service of queries arriving at `arrivals` (s) with
+    service times `service` (s): (latencies in ms, served queries/s)."""
+    done, lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        done = max(a, done) + sv
+        lat.append((done - a) * 1000.0)
+    return lat, len(lat) / (done - arrivals[0]) if len(lat) else None
 
-    import geminigraph_gb300 as gg
-    device = dist.local_rank
-    rng = np.random.default_rng(SEED + 77)
-    scales, probs = (20, 22, 24, 26), (0.4, 0.3, 0.2, 0.1)
-    t0 = time.perf_counter()
-    graphs = [gg.Graph.generate(gg.RMAT, sc, 16, SEED + i, weighted=True, device=device) for i, sc in enumerate(scales)]
-    build_s = time.perf_counter() - t0
-    bins = [tune_bins(g, args) for g in graphs]
-    degs = [g.out_degree() for g in graphs]
-    n = args.queries
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
-    gsel = rng.choice(len(scales), size=n, p=probs)
-    kinds = (rng.random(n) < 0.25).astype(int)
-    roots = [gg.pick_roots(degs[j], 1, int(rng.integers(1 << 30)))[0] for j in gsel]
-    queries = list(zip(gsel.tolist(), kinds.tolist(), roots))
-    # warm-up: one batch per (graph, kind) opens the pools' code paths
-    server = gg.Server(device=device)
-    ids = [server.add_graph(g) for g in graphs]
-    for j in range(len(graphs)):
-        for k in (0, 1):
-            server.submit(ids[j], k, gg.pick_roots(degs[j], 1, 5)[0])
-    got = 0
-    while got < 2 * len(graphs):
-        got += len(server.wait(timeout_ms=1000))
-    clocks = ClockSampler(device)
-    clocks.start()
-    results = {}
-    tickets = {}
+
+def serve_stream(gg, server, ids, queries, arrivals):
+    """Submits queries[i] at arrivals[i] (s after the start) from a client
+    thread and collects the results: (results by query index, span in s)."""
+    import threading
+    results, tickets = {}, {}
 
     def client():
         start = time.perf_counter()
@@ -876,20 +856,41 @@ def gpu_arm_serve(args, dist):
     wall0 = time.perf_counter()
     th = threading.Thread(target=client)
     th.start()
-    while len(results) < n:
+    while len(results) < len(queries):
         for r in server.wait(max_results=1024, timeout_ms=50):
             results[r["ticket"]] = r
-        if not th.is_alive() and len(results) >= n:
-            break
     th.join()
     span = time.perf_counter() - wall0
-    clk = clocks.stop()
-    st = server.stats()
-    served = {tickets[t]: r for t, r in results.items()}
-    lat = [served[i]["latency_ms"] for i in range(n)]
-    # plain: the first args.plain queries one at a time, FIFO on the same arrivals
+    return {tickets[t]: r for t, r in results.items()}, span
+
+
+def gpu_arm_serve(args, dist):
+    """One step = one query of the stream.  value = completed queries / the
+    span from the first arrival to the last completion of a stream offered at
+    args.rate (the server's capacity when that rate is above it).  The same
+    query mix is then offered at 50% and 90% of that capacity, with and
+    without a batch window on the SSSP pools, for p50/p99 service latency.
+    plain = the first args.plain queries run one at a time through gg_bfs /
+    gg_sssp (device time as service time), replayed FIFO on each stream's
+    arrival times."""
+    import geminigraph_gb300 as gg
+    device = dist.local_rank
+    rng = np.random.default_rng(SEED + 77)
+    scales, probs = (20, 22, 24, 26), (0.4, 0.3, 0.2, 0.1)
+    t0 = time.perf_counter()
+    graphs = [gg.Graph.generate(gg.RMAT, sc, 16, SEED + i, weighted=True, device=device) for i, sc in enumerate(scales)]
+    build_s = time.perf_counter() - t0
+    bins = [tune_bins(g, args) for g in graphs]
+    degs = [g.out_degree() for g in graphs]
+    n = args.queries
+    unit = rng.exponential(1.0, n)          # arrival gaps at rate 1, scaled per stream
+    gsel = rng.choice(len(scales), size=n, p=probs)
+    kinds = (rng.random(n) < 0.25).astype(int)
+    roots = [gg.pick_roots(degs[j], 1, int(rng.integers(1 << 30)))[0] for j in gsel]
+    queries = list(zip(gsel.tolist(), kinds.tolist(), roots))
+    # plain service times and checksums of the first queries, one at a time
     m = min(args.plain, n)
-    done_t, plain_lat, mism = 0.0, [], 0
+    plain_svc, plain_chk = [], []
     for i in range(m):
         j, k, r = queries[i]
         g = graphs[j]
@@ -899,35 +900,70 @@ def gpu_arm_serve(args, dist):
         else:
             d1, s1 = g.sssp(r)
             chk = gg.result_checksum(d1, 1)
-        svc = s1.device_ms / 1000.0
-        begin = max(arrivals[i], done_t)
-        done_t = begin + svc
-        plain_lat.append((done_t - arrivals[i]) * 1000.0)
-        mism += int(chk != served[i]["checksum"])
-    plain_qps = m / (done_t - arrivals[0]) if m else None
-    value = n / span
+        plain_svc.append(s1.device_ms / 1000.0)
+        plain_chk.append(chk)
+
+    def new_server(window_ms=0.0):
+        server = gg.Server(device=device)
+        server.set_solo(args.solo)
+        ids = [server.add_graph(g) for g in graphs]
+        if window_ms:
+            server.set_window(gg.Server.SSSP, window_ms)
+        # warm-up: one query per (graph, kind) opens the pools' code paths
+        for j in range(len(graphs)):
+            for k in (0, 1):
+                server.submit(ids[j], k, gg.pick_roots(degs[j], 1, 5)[0])
+        got = 0
+        while got < 2 * len(graphs):
+            got += len(server.wait(timeout_ms=1000))
+        return server, ids
+
+    def run(rate, count, window_ms=0.0):
+        server, ids = new_server(window_ms)
+        arr = np.cumsum(unit[:count]) / rate
+        served, span = serve_stream(gg, server, ids, queries[:count], arr)
+        st = server.stats()
+        server.close()
+        lat = [served[i]["latency_ms"] for i in range(count)]
+        mism = sum(int(plain_chk[i] != served[i]["checksum"]) for i in range(min(m, count)))
+        plat, pqps = fifo_replay(arr[:m], plain_svc[:count])
+        return {"offered_qps": round(rate, 1), "queries": count, "served_qps": round(count / span, 1),
+                "p50_ms": round(pct(lat, 50), 3), "p99_ms": round(pct(lat, 99), 3),
+                "window_ms": window_ms, "checksum_mismatches": mism,
+                "plain": {"served_qps": round(pqps, 1) if pqps else None, "p50_ms": round(pct(plat, 50), 3),
+                          "p99_ms": round(pct(plat, 99), 3), "queries": min(m, count)},
+                "server": {k: st[k] for k in ("pools_opened", "pools_closed", "admission_waits", "max_busy_pools",
+                                              "max_lanes_in_use", "solo_runs")}}
+
+    clocks = ClockSampler(device)
+    clocks.start()
+    over = run(args.rate, n)
+    capacity = over["served_qps"]
+    loads = [run(f * capacity, min(n, args.load_queries), w) for f in (0.5, 0.9) for w in (0.0, args.window)]
+    clk = clocks.stop()
+    value = capacity
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": args.gpus, "steps": n,
-        "warmup": 2 * len(graphs), "ms_per_step": round(span * 1000 / n, 4), "higher_is_better": True,
+        "warmup": 2 * len(graphs), "ms_per_step": round(1000.0 / value, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 lane masks / f32",
         "data": "synthetic (seeded R-MAT generated on the device; Poisson query stream)",
         "config": {"workload": WORKLOADS["serve"]["desc"], "queries": n, "rate_qps": args.rate,
+                   "sssp_solo_below": args.solo,
                    "graph_build_s": round(build_s, 2), "parallelism": f"replicas x{args.gpus}",
                    "bins": [{k: b[k] for k in ("source", "light_deg", "pull_chunk", "pull_vector", "l1_hot_bytes")}
                             for b in bins]},
-        "latency_ms": {"p50": round(pct(lat, 50), 3), "p99": round(pct(lat, 99), 3)},
-        "plain": {"value": round(plain_qps, 1) if plain_qps else None, "unit": "queries/s",
-                  "latency_ms": {"p50": round(pct(plain_lat, 50), 3), "p99": round(pct(plain_lat, 99), 3)},
-                  "what": f"first {m} queries one at a time through gg_bfs / gg_sssp, FIFO on the same arrivals"},
-        "speedup_vs_plain": round(value / plain_qps, 2) if plain_qps else None,
-        "checksum_mismatches": mism, "checked": m,
-        "server": {k: st[k] for k in ("pools_opened", "pools_closed", "admission_waits", "max_busy_pools",
-                                      "max_lanes_in_use")},
+        "latency_ms": {"p50": over["p50_ms"], "p99": over["p99_ms"],
+                       "note": "offered above capacity: queueing time"},
+        "plain": dict(over["plain"], what=f"first {m} queries one at a time through gg_bfs / gg_sssp (device "
+                                          "time), FIFO on the same arrivals"),
+        "speedup_vs_plain": round(value / over["plain"]["served_qps"], 2) if over["plain"]["served_qps"] else None,
+        "checksum_mismatches": over["checksum_mismatches"], "checked": min(m, n),
+        "server": over["server"],
+        "loads": loads,
         "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 4,
                 "d2h_bytes_per_step": 16, "note": "per query the root in and reached count + checksum out"},
         "clocks": clk,
     }
-    server.close()
     if args.mix:
         line["mix_ceiling"] = serve_mix_ceiling(gg, graphs, degs, scales, probs)
     if dist.rank == 0:
@@ -1027,6 +1063,12 @@ def main():
     ap.add_argument("--queries", type=int, default=2000, help="serve: queries in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: mean arrival rate (queries/s)")
     ap.add_argument("--plain", type=int, default=300, help="serve: queries replayed one at a time")
+    ap.add_argument("--load-queries", type=int, default=1000,
+                    help="serve: queries per stream offered at 50%% and 90%% of the measured capacity")
+    ap.add_argument("--solo", type=int, default=16,
+                    help="serve: idle SSSP pools with fewer waiting queries run them one at a time (0: always batch)")
+    ap.add_argument("--window", type=float, default=5.0,
+                    help="serve: SSSP batch window (ms) of the second stream at each offered load")
     ap.add_argument("--mix", action="store_true",
                     help="serve: also time plain and full-batch queries per graph and kind (the mix's ceiling)")
     args = ap.parse_args()

@@ -96,11 +96,14 @@ def library():
         "gg_server_wait": ([vp, ctypes.POINTER(_QueryResult), i32, i32, ctypes.POINTER(i32)], i32),
         "gg_server_stats_get": ([vp, ctypes.POINTER(_ServerStats)], i32),
         "gg_server_free": ([vp], i32),
+        "gg_server_set_window": ([vp, i32, ctypes.c_double], i32),
+        "gg_server_set_solo": ([vp, i32], i32),
         "gg_pool_bytes": ([vp, i32], u64),
         "gg_graph_set_bins": ([vp, u32, u32, u32], i32),
         "gg_bfs_many": ([vp, vp, i32, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_sssp_delta": ([vp, ctypes.c_float], i32),
         "gg_graph_set_batched_switch": ([vp, u32], i32),
+        "gg_graph_set_batched_thread_lanes": ([vp, u32], i32),
         "gg_dump_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
@@ -137,7 +140,8 @@ class _ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_uint64), ("pending", ctypes.c_uint64), ("pools_open", ctypes.c_uint64),
                 ("pools_opened", ctypes.c_uint64), ("pools_closed", ctypes.c_uint64),
                 ("admission_waits", ctypes.c_uint64), ("bytes_in_use", ctypes.c_uint64), ("budget", ctypes.c_uint64),
-                ("max_busy_pools", ctypes.c_int32), ("max_lanes_in_use", ctypes.c_int32)]
+                ("max_busy_pools", ctypes.c_int32), ("max_lanes_in_use", ctypes.c_int32),
+                ("solo_runs", ctypes.c_uint64)]
 
 
 class _TuneResult(ctypes.Structure):
@@ -319,6 +323,11 @@ class Graph:
 
     def set_batched_switch(self, divisor):
         _check(library().gg_graph_set_batched_switch(self.h, int(divisor)))
+
+    def set_batched_thread_lanes(self, lanes):
+        """Batched SSSP steps with at most this many lanes in flight relax
+        edges one thread per edge (gg_graph_set_batched_thread_lanes)."""
+        _check(library().gg_graph_set_batched_thread_lanes(self.h, int(lanes)))
 
     def set_sssp_delta(self, delta):
         _check(library().gg_graph_set_sssp_delta(self.h, float(delta)))
@@ -510,6 +519,14 @@ class Server:
     @staticmethod
     def pool_bytes(graph, kind):
         return int(library().gg_pool_bytes(graph.h, kind))
+
+    def set_solo(self, below):
+        """Idle SSSP pools with fewer waiting queries run them alone (gg_server_set_solo)."""
+        _check(library().gg_server_set_solo(self.h, int(below)))
+
+    def set_window(self, kind, window_ms):
+        """Batch window of the kind's pools (gg_server_set_window)."""
+        _check(library().gg_server_set_window(self.h, kind, float(window_ms)))
 
     def add_graph(self, graph):
         gid = ctypes.c_int32()

@@ -700,6 +700,76 @@ __global__ void __launch_bounds__(PUSH_THREADS)
   ms_flush(mc, t_alive, t_edges, 0);
 }
 
+// The same relaxation, one thread per edge, looping over the SSSP lanes in
+// which the source is on the frontier: for steps with few lanes in flight,
+// where a warp per edge would leave most of its threads idle.
+__global__ void __launch_bounds__(PUSH_THREADS)
+    msp_push_thread(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
+                    unsigned long long total, Dir d, const u64 *__restrict__ front, u64 *next, float *dist,
+                    uint32_t *q_out, MsCounters *mc) {
+  __shared__ unsigned long long s_P[PUSH_STAGE + 1];
+  __shared__ unsigned long long s_base[PUSH_STAGE];
+  __shared__ uint32_t s_src[PUSH_STAGE];
+  __shared__ uint32_t s_lo, s_hi;
+  const unsigned long long ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
+  u64 t_alive = 0, t_edges = 0;
+  for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const unsigned long long e0 = tile * PUSH_TILE;
+    const unsigned long long e1 = e0 + PUSH_TILE < total ? e0 + PUSH_TILE : total;
+    if (threadIdx.x == 0) {
+      uint32_t lo = upper_bound_idx<unsigned long long>(P, 0, n + 1, e0) - 1;
+      s_lo = lo;
+      s_hi = upper_bound_idx<unsigned long long>(P, lo, n + 1, e1 - 1);
+    }
+    __syncthreads();
+    const uint32_t lo = s_lo, hi = s_hi, cnt = hi - lo;
+    const bool staged = cnt <= (uint32_t)PUSH_STAGE;
+    if (staged) {
+      for (uint32_t i = threadIdx.x; i < cnt; i += PUSH_THREADS) {
+        const unsigned long long pi = P[lo + i];
+        const uint32_t src = q[lo + i];
+        s_P[i] = pi;
+        s_src[i] = src;
+        s_base[i] = d.off[src] - pi;
+      }
+    }
+    __syncthreads();
+    for (unsigned long long e = e0 + threadIdx.x; e < e1; e += PUSH_THREADS) {
+      uint32_t u;
+      unsigned long long k;
+      if (staged) {
+        const uint32_t i = upper_bound_idx<unsigned long long>(s_P, 0, cnt, e) - 1;
+        u = s_src[i];
+        k = s_base[i] + e;
+      } else {
+        const uint32_t i = upper_bound_idx<unsigned long long>(P, lo, hi, e) - 1;
+        u = q[i];
+        k = d.off[u] + (e - P[i]);
+      }
+      const uint32_t v = d.nbr[k];
+      const float wt = d.w[k];
+      u64 fm = front[u], low = 0;
+      while (fm) {
+        const int l = __ffsll((long long)fm) - 1;
+        fm &= fm - 1;
+        const float nd = __fadd_rn(dist[(size_t)u * LANES + l], wt);
+        float *p = dist + (size_t)v * LANES + l;
+        if (nd < *(volatile float *)p && atomic_min_float_b(p, nd)) low |= 1ull << l;
+      }
+      if (low) {
+        const u64 old = atomicOr(next + v, low);
+        if (!old) {
+          q_out[atomicAdd(&mc->qlen, 1u)] = v;
+          t_edges += d.deg[v];
+        }
+        t_alive |= low;
+      }
+    }
+    __syncthreads();
+  }
+  ms_flush(mc, t_alive, t_edges, 0);
+}
+
 }  // namespace gg
 
 // ---------------------------------------------------------------- LanePool
@@ -950,7 +1020,8 @@ int LanePool::sssp_step() {
     GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
                                                                scan64_, s_, &launches)));
     if (tr_) GG_TRY(tr_->kbegin());
-    msp_push<<<push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
+    (__builtin_popcountll(active_) <= (int)g_->batched_thread_lanes ? msp_push_thread : msp_push)<<<
+        push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
                                                               dist_, q_[cur_ ^ 1], mc_);
     if (tr_) GG_TRY(tr_->kend());
     launches += 1;
@@ -1013,7 +1084,8 @@ int LanePool::sssp_bucket_step() {
     GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
                                                                scan64_, s_, &launches)));
     if (tr_) GG_TRY(tr_->kbegin());
-    msp_push<<<push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
+    (__builtin_popcountll(active_) <= (int)g_->batched_thread_lanes ? msp_push_thread : msp_push)<<<
+        push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
                                                               dist_, q_[cur_ ^ 1], mc_);
     if (tr_) GG_TRY(tr_->kend());
     launches += 1;
@@ -1208,6 +1280,15 @@ extern "C" int gg_graph_set_batched_switch(gg_graph *g, uint32_t divisor) {
     return GG_ERR_INVALID;
   }
   g->batched_switch_div = divisor ? divisor : 20;
+  return GG_OK;
+}
+
+extern "C" int gg_graph_set_batched_thread_lanes(gg_graph *g, uint32_t lanes) {
+  if (!g || lanes > 64) {
+    set_error("need a graph and at most 64 lanes");
+    return GG_ERR_INVALID;
+  }
+  g->batched_thread_lanes = lanes;
   return GG_OK;
 }
 

@@ -183,6 +183,9 @@ struct gg_graph {
   // batched BFS steps pull (dense) when the union frontier's out-edges reach
   // edges / batched_switch_div, else push
   uint32_t batched_switch_div = 20;
+  // batched SSSP steps with at most this many lanes in flight relax edges
+  // one thread per edge (msp_push_thread) instead of one warp per edge
+  uint32_t batched_thread_lanes = 16;
   int wmin_known = 0;
   float wmin = 0.0f;
   // reduction pulls on the hot-source layout: gathered state of the first

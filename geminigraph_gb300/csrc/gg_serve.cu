@@ -6,7 +6,9 @@
 // concurrently on the device.  A worker admits waiting queries into free
 // lanes between iterations, runs one iteration of all its lanes, and retires
 // the lanes whose frontier emptied, reporting each query's reached count and
-// result checksum (gg_result_checksum).  A pool is opened only when its
+// result checksum (gg_result_checksum).  An idle pool may hold its first
+// queries for a batch window so that more start together (gg_server_set_window).
+// A pool is opened only when its
 // buffers fit in the server's HBM budget and in the device's free memory;
 // otherwise its queries wait until an idle pool closes and frees memory.
 #include <chrono>
@@ -17,9 +19,28 @@
 #include <thread>
 #include <vector>
 
+#include "gg_gen.h"
 #include "gg_lanes.cuh"
 
 namespace gg {
+
+// Reached count and gg_result_checksum (kind 1) of one distance array.
+__global__ void solo_digest(const float *__restrict__ dist, uint32_t V, unsigned long long *out) {
+  unsigned long long c = 0, h = 0;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x) {
+    const float d = dist[v];
+    if (d < 1e9f) {
+      c += 1;
+      h += gg_mix64((unsigned long long)v * 0x9E3779B97F4A7C15ull + __float_as_uint(d));
+    }
+  }
+  c = warp_sum(c);
+  h = warp_sum(h);
+  if (lane_id() == 0) {
+    atomicAdd(out, c);
+    atomicAdd(out + 1, h);
+  }
+}
 
 static double now_ms() {
   using namespace std::chrono;
@@ -36,6 +57,7 @@ struct Query {
 struct PoolSlot {
   LanePool *pool = nullptr;
   size_t bytes = 0;
+  unsigned long long *solo_out = nullptr;  // device: reached, checksum of a solo run
   std::deque<Query> pending;
   Query lane_q[POOL_LANES];
   std::thread worker;
@@ -51,6 +73,12 @@ struct gg_server {
   uint64_t budget = 0, used = 0;
   uint64_t reserve = 2ull << 30;  // device memory left free for the graphs' own calls
   double idle_close_ms = 200.0;
+  // batch window per kind: an idle pool waits up to this long after its
+  // oldest waiting query for more queries to start with it (0: start at once)
+  double window_ms[2] = {0.0, 0.0};
+  // an idle SSSP pool with fewer waiting queries than this runs them one at
+  // a time through the single-root SSSP (0: always batch)
+  int sssp_solo_below = 16;
   std::vector<gg_graph *> graphs;
   std::map<std::pair<int, int>, PoolSlot *> pools;
   std::mutex mu;
@@ -60,9 +88,41 @@ struct gg_server {
   bool stop = false;
   int error = GG_OK;
   // statistics
-  uint64_t completed = 0, pools_opened = 0, pools_closed = 0, admission_waits = 0;
+  uint64_t completed = 0, pools_opened = 0, pools_closed = 0, admission_waits = 0, solo_runs = 0;
   int busy_pools = 0, max_busy_pools = 0, max_lanes_in_use = 0, lanes_in_use = 0;
 };
+
+// One query through the single-root SSSP (gg_sssp) on the graph's own
+// stream; its distances are digested on the device.  Only this pool's worker
+// calls single-root code on the graph while the server runs.
+static int solo_sssp(gg_server *S, gg_graph *g, PoolSlot *slot, const Query &q) {
+  if (!slot->solo_out) GG_CUDA(cudaMalloc(&slot->solo_out, 2 * sizeof(unsigned long long)));
+  gg_run_stats st;
+  memset(&st, 0, sizeof(st));
+  GG_TRY(gg_sssp(g, q.root, nullptr, &st));
+  GG_CUDA(cudaMemsetAsync(slot->solo_out, 0, 2 * sizeof(unsigned long long), g->stream));
+  solo_digest<<<grid_for(g->V, 256, g->num_sms, 8), 256, 0, g->stream>>>((const float *)g->result[0], g->V,
+                                                                         slot->solo_out);
+  unsigned long long h[2];
+  GG_CUDA(cudaMemcpyAsync(h, slot->solo_out, sizeof(h), cudaMemcpyDeviceToHost, g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  gg_query_result r;
+  r.ticket = q.ticket;
+  r.graph = q.graph;
+  r.kind = q.kind;
+  r.root = q.root;
+  r.status = GG_OK;
+  r.reached = h[0];
+  r.checksum = h[1];
+  r.active_edges = 0;
+  r.latency_ms = now_ms() - q.t_submit;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->done.push_back(r);
+  S->completed += 1;
+  S->solo_runs += 1;
+  S->cv_done.notify_all();
+  return GG_OK;
+}
 
 static void worker_loop(gg_server *S, std::pair<int, int> key, PoolSlot *slot) {
   cudaSetDevice(S->device);
@@ -97,6 +157,23 @@ static void worker_loop(gg_server *S, std::pair<int, int> key, PoolSlot *slot) {
         counted_busy = true;
         if (S->busy_pools > S->max_busy_pools) S->max_busy_pools = S->busy_pools;
       }
+      // solo: too few SSSP queries for a batch to beat single-root runs
+      if (kind == LanePool::SSSP && !slot->pool->active() && !slot->pending.empty() &&
+          (int)slot->pending.size() < S->sssp_solo_below) {
+        const Query q = slot->pending.front();
+        slot->pending.pop_front();
+        lk.unlock();
+        int st = solo_sssp(S, g, slot, q);
+        lk.lock();
+        if (st != GG_OK) {
+          S->error = st;
+          S->stop = true;
+          S->cv_done.notify_all();
+          break;
+        }
+        idle_since = now_ms();
+        continue;
+      }
       // admission: the pool's buffers must fit the budget and the free memory
       if (!slot->pool->is_open()) {
         size_t free_b = 0, total_b = 0;
@@ -119,6 +196,16 @@ static void worker_loop(gg_server *S, std::pair<int, int> key, PoolSlot *slot) {
       }
       const unsigned long long free_lanes = ~slot->pool->used();
       int nfree = __builtin_popcountll(free_lanes);
+      // batch window: an idle pool that cannot fill its lanes yet waits for
+      // more queries, until the oldest has waited window_ms
+      const double win = S->window_ms[key.second];
+      if (win > 0.0 && !slot->pool->active() && !slot->pending.empty() && (int)slot->pending.size() < nfree) {
+        const double left = slot->pending.front().t_submit + win - now_ms();
+        if (left > 0.0) {
+          S->cv_work.wait_for(lk, std::chrono::microseconds((long long)(left * 1000.0) + 1));
+          continue;
+        }
+      }
       while (nfree > 0 && !slot->pending.empty()) {
         take.push_back(slot->pending.front());
         slot->pending.pop_front();
@@ -202,6 +289,26 @@ int gg_server_create(int device, uint64_t hbm_budget, gg_server **out) {
   S->device = device;
   S->budget = hbm_budget ? hbm_budget : (free_b > S->reserve ? free_b - S->reserve : 0);
   *out = S;
+  return GG_OK;
+}
+
+int gg_server_set_solo(gg_server *S, int below) {
+  if (!S || below < 0 || below > POOL_LANES) {
+    set_error("need a server and 0..64 queries");
+    return GG_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->sssp_solo_below = below;
+  return GG_OK;
+}
+
+int gg_server_set_window(gg_server *S, int kind, double window_ms) {
+  if (!S || (kind != 0 && kind != 1) || !(window_ms >= 0.0)) {
+    set_error("need a server, kind 0 (BFS) or 1 (SSSP) and a window >= 0");
+    return GG_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->window_ms[kind] = window_ms;
   return GG_OK;
 }
 
@@ -316,6 +423,7 @@ int gg_server_stats_get(gg_server *S, gg_server_stats *st) {
   st->budget = S->budget;
   st->max_busy_pools = S->max_busy_pools;
   st->max_lanes_in_use = S->max_lanes_in_use;
+  st->solo_runs = S->solo_runs;
   return GG_OK;
 }
 
@@ -329,6 +437,7 @@ int gg_server_free(gg_server *S) {
   for (auto &kv : S->pools)
     if (kv.second->started) kv.second->worker.join();
   for (auto &kv : S->pools) {
+    if (kv.second->solo_out) cudaFree(kv.second->solo_out);
     delete kv.second->pool;
     delete kv.second;
   }

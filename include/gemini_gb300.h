@@ -247,6 +247,14 @@ int gg_graph_set_batched_switch(gg_graph *g, uint32_t divisor);
  * next starts from empty. */
 int gg_graph_set_sssp_delta(gg_graph *g, float delta);
 
+/* Batched SSSP (gg_sssp_batched and the serving pools; no reference
+ * counterpart): a step with at most `lanes` traversals in flight relaxes each
+ * edge in one thread, looping over the source's lanes, instead of one warp
+ * per edge covering all 64 lanes.  0 always uses the warp form.  Distances
+ * do not depend on it.  Default 16 (measured: with 16 lanes the thread form
+ * is faster at R-MAT 20-26, with 64 the warp form). */
+int gg_graph_set_batched_thread_lanes(gg_graph *g, uint32_t lanes);
+
 /* Batched betweenness centrality (no reference counterpart; per lane the
  * computation of toolkits/bc.cpp:24-196): up to 64 roots in one pass per
  * level.  dependencies and inv_num_paths (either may be NULL) receive
@@ -296,6 +304,7 @@ typedef struct {
   uint64_t bytes_in_use, budget;
   int32_t max_busy_pools;    /* most pools running at once */
   int32_t max_lanes_in_use;  /* most queries on the device at once */
+  uint64_t solo_runs;        /* SSSP queries run alone (gg_server_set_solo) */
 } gg_server_stats;
 
 /* Device bytes one pool of kind (0 BFS, 1 SSSP) on g holds while open. */
@@ -303,6 +312,21 @@ uint64_t gg_pool_bytes(const gg_graph *g, int kind);
 /* hbm_budget: device bytes the pools may hold (0 = free memory less 2 GiB). */
 int gg_server_create(int device, uint64_t hbm_budget, gg_server **out);
 /* The graph must outlive the server; calls on it must not overlap serving. */
+/* Batch window of the pools of one kind (0 BFS, 1 SSSP): a pool with no
+ * traversal running and fewer waiting queries than free lanes holds them up
+ * to window_ms after the oldest one arrived, so that more queries start in
+ * the same steps.  0 (the default) starts them at once.  Results do not
+ * depend on it; latency does. */
+int gg_server_set_window(gg_server *s, int kind, double window_ms);
+/* An SSSP pool with no traversal running and fewer than `below` waiting
+ * queries runs them one at a time through the single-root SSSP (gg_sssp, on
+ * the graph's own stream) instead of starting a batch: a batched SSSP step
+ * costs nearly as much with a few lanes as with 64, so small batches are
+ * slower than single-root runs (R-MAT 26: 257 ms for one lane against 75 ms
+ * alone; batches pass single-root runs near 20 lanes).  0 always batches.
+ * Default 16.  While a server runs, only it may call single-root toolkits on
+ * its graphs. */
+int gg_server_set_solo(gg_server *s, int below);
 int gg_server_add_graph(gg_server *s, gg_graph *g, int *graph_id);
 int gg_server_submit(gg_server *s, int graph_id, int kind, uint32_t root, uint64_t *ticket);
 /* Up to max_results completed queries; waits up to timeout_ms for the first. */

@@ -68,6 +68,24 @@ def test_sssp_batched_lanes_equal_single_runs(case, n):
         assert int(reached[i]) == int((single < np.float32(1e9)).sum())
 
 
+@pytest.mark.parametrize("thread_lanes", [0, 64])
+def test_sssp_batched_push_forms_agree(case, thread_lanes):
+    """Warp-per-edge (0) and thread-per-edge (64: every step) relaxation give
+    every lane the single-root distances bit for bit."""
+    V, s, d, w, g = case
+    g.set_batched_thread_lanes(thread_lanes)
+    try:
+        roots = roots_for(V, s, 20, seed=70)
+        dist, reached, st = gg.sssp_batched(g, roots)
+    finally:
+        g.set_batched_thread_lanes(16)
+    for i, r in enumerate(roots):
+        single, _ = g.sssp(r)
+        assert np.array_equal(dist[i].view(np.uint32), single.view(np.uint32)), f"lane {i} root {r}"
+    with pytest.raises(gg.GeminiError):
+        g.set_batched_thread_lanes(65)
+
+
 def test_batched_argument_errors(case):
     V, s, d, w, g = case
     with pytest.raises(ValueError):

@@ -51,9 +51,13 @@ def run_queries(server, queries, burst=37, pause=0.002):
     return tickets, done
 
 
-def test_served_results_equal_single_root_runs(graphs):
+@pytest.mark.parametrize("solo", [0, 16, 64])
+def test_served_results_equal_single_root_runs(graphs, solo):
+    """solo = 0: every SSSP query in a batch; 16 (default) / 64: an idle SSSP
+    pool with fewer waiting queries runs them alone through gg_sssp."""
     rng = np.random.default_rng(3)
     server = gg.Server()
+    server.set_solo(solo)
     ids = [server.add_graph(g) for g, _, _ in graphs]
     queries = []
     for _ in range(400):
@@ -74,8 +78,33 @@ def test_served_results_equal_single_root_runs(graphs):
         assert r["graph"] == gid and r["kind"] == kind and r["root"] == root
     st = server.stats()
     assert st["completed"] == len(queries)
+    assert (st["solo_runs"] > 0) == (solo > 0)
     assert st["max_lanes_in_use"] > 1         # queries shared the device
     assert st["max_busy_pools"] > 1           # pools of different graphs/kinds overlapped
+    server.close()
+
+
+def test_batch_window_keeps_results(graphs):
+    """Idle pools that hold their first queries for a batch window start them
+    together; every result still equals the query's single-root run."""
+    rng = np.random.default_rng(9)
+    server = gg.Server()
+    server.set_window(gg.Server.SSSP, 4.0)
+    server.set_window(gg.Server.BFS, 1.0)
+    ids = [server.add_graph(g) for g, _, _ in graphs]
+    queries = []
+    for _ in range(150):
+        j = int(rng.integers(0, len(graphs)))
+        g, V, deg = graphs[j]
+        queries.append((ids[j], int(rng.integers(0, 2)), gg.pick_roots(deg, 1, int(rng.integers(1 << 30)))[0]))
+    tickets, done = run_queries(server, queries, burst=5, pause=0.003)
+    for t, (gid, kind, root) in tickets.items():
+        assert (done[t]["reached"], done[t]["checksum"]) == expected(graphs[gid][0], kind, root)
+    assert server.stats()["max_lanes_in_use"] > 1
+    with pytest.raises(gg.GeminiError):
+        server.set_window(2, 1.0)
+    with pytest.raises(gg.GeminiError):
+        server.set_window(0, -1.0)
     server.close()
 
 

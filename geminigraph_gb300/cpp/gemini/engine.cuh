@@ -33,6 +33,23 @@
 // began.  R is the sum of the slots' returns (integer or floating point).
 // One partition: dense_selective is accepted and ignored, as the reference
 // does for partitions == 1 (core/graph.hpp:1662).
+//
+// List form, for callbacks written the reference's way (a slot or a dense
+// signal that walks a VertexAdjList with a loop of its own):
+//   process_edges<R, M>(sparse_signal(v), sparse_slot(src, msg, VertexAdjList),
+//                       dense_signal(dst, VertexAdjList), dense_slot(dst, msg),
+//                       active)
+// with the reference's argument lists (core/graph.hpp:1493-1494).  Callbacks
+// are __device__ lambdas capturing by value (device lambdas cannot capture
+// by reference); signals call graph->emit(v, msg) on the DeviceGraph of
+// Engine::device_graph(), and the device forms of cas / write_min /
+// write_add below are at hand.  Each callback call gets a piece of at most
+// LIST_PIECE consecutive entries of one list, so a long list is handed over
+// in several calls -- as the reference itself does when a vertex's edges are
+// split over sockets or partitions (core/graph.hpp:1614-1658, 1755-1789),
+// where a dense signal may emit one partial message per part and the dense
+// slot combines them.  Minima, first-hit CAS and write_add slots (the five
+// toolkits) give the single-call results; sums differ in order only.
 #ifndef GEMINI_GB300_ENGINE_CUH
 #define GEMINI_GB300_ENGINE_CUH
 
@@ -45,6 +62,39 @@
 #include <vector>
 
 #include "gemini/graph.hpp"
+
+// Device forms of the reference's atomics (core/atomic.hpp:24-51), for the
+// list form's callbacks: compare-and-swap on 4- or 8-byte values, and the
+// min / add loops built on it.
+template <class T>
+__device__ inline bool cas(T *ptr, T old_val, T new_val) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cas works on 4- or 8-byte values");
+  if constexpr (sizeof(T) == 4) {
+    unsigned o, n;
+    memcpy(&o, &old_val, 4);
+    memcpy(&n, &new_val, 4);
+    return atomicCAS(reinterpret_cast<unsigned *>(ptr), o, n) == o;
+  } else {
+    unsigned long long o, n;
+    memcpy(&o, &old_val, 8);
+    memcpy(&n, &new_val, 8);
+    return atomicCAS(reinterpret_cast<unsigned long long *>(ptr), o, n) == o;
+  }
+}
+template <class T>
+__device__ inline bool write_min(T *ptr, T val) {
+  T cur = *reinterpret_cast<volatile T *>(ptr);
+  while (cur > val) {
+    if (cas(ptr, cur, val)) return true;
+    cur = *reinterpret_cast<volatile T *>(ptr);
+  }
+  return false;
+}
+template <class T>
+__device__ inline void write_add(T *ptr, T val) {
+  T cur = *reinterpret_cast<volatile T *>(ptr);
+  while (!cas(ptr, cur, (T)(cur + val))) cur = *reinterpret_cast<volatile T *>(ptr);
+}
 
 namespace gemini {
 
@@ -417,6 +467,101 @@ __global__ void __launch_bounds__(THREADS)
   block_reduce_add(r, out);
 }
 
+// ---- list form (process_edges with VertexAdjList callbacks)
+constexpr uint64_t LIST_PIECE = 64;  // entries per callback call at most
+
+template <typename E>
+__global__ void interleave_adjacency(const uint32_t *__restrict__ nbr, const float *__restrict__ w, uint64_t n,
+                                     AdjUnit<E> *__restrict__ out) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    AdjUnit<E> a;
+    a.neighbour = nbr[k];
+    a.edge_data = w[k];
+    out[k] = a;
+  }
+}
+
+// Sparse signals: every active vertex (they emit through the DeviceGraph).
+template <class SS>
+__global__ void __launch_bounds__(THREADS)
+    list_sparse_signal(const unsigned long long *__restrict__ bm, size_t words, uint32_t V, SS ss) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long w = bm[i];
+    while (w) {
+      const int b = __ffsll((long long)w) - 1;
+      w &= w - 1;
+      const size_t v = i * 64 + b;
+      if (v < V) ss((uint32_t)v);
+    }
+  }
+}
+
+// Sparse slots: the out-edges of the emitted messages, cut into pieces of
+// LIST_PIECE entries of the messages' concatenated lists (pre = prefix of
+// their out-degrees); a piece calls the slot once per message it covers.
+template <typename R, typename M, typename E, class SL>
+__global__ void __launch_bounds__(THREADS)
+    list_sparse_slot(AdjUnit<E> *adj, const uint64_t *__restrict__ off, const uint32_t *__restrict__ qv,
+                     const M *__restrict__ qm, const unsigned long long *__restrict__ pre, size_t n, SL sl, R *out) {
+  const unsigned long long total = pre[n];
+  const unsigned long long pieces = (total + LIST_PIECE - 1) / LIST_PIECE;
+  R r = R(0);
+  for (unsigned long long p = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; p < pieces;
+       p += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long e0 = p * LIST_PIECE, e1 = e0 + LIST_PIECE < total ? e0 + LIST_PIECE : total;
+    size_t lo = 0, hi = n;  // first message index with pre > e0, in (0, n]
+    while (lo < hi) {
+      const size_t mid = (lo + hi) >> 1;
+      if (pre[mid] <= e0)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    for (size_t i = lo - 1; i < n && pre[i] < e1; i++) {
+      const unsigned long long a = pre[i] > e0 ? pre[i] : e0, b = pre[i + 1] < e1 ? pre[i + 1] : e1;
+      if (a >= b) continue;
+      const uint32_t src = qv[i];
+      AdjUnit<E> *base = adj + (off[src] - pre[i]);
+      r += sl(src, qm[i], VertexAdjList<E>(base + a, base + b));
+    }
+  }
+  block_reduce_add(r, out);
+}
+
+// Dense signals: the in-lists cut into pieces of LIST_PIECE consecutive
+// entries of the CSC; a piece calls the signal once per vertex it covers.
+template <typename E, class DS>
+__global__ void __launch_bounds__(THREADS)
+    list_dense_signal(AdjUnit<E> *adj, const uint64_t *__restrict__ off, uint32_t V, uint64_t entries, DS ds) {
+  const unsigned long long pieces = (entries + LIST_PIECE - 1) / LIST_PIECE;
+  for (unsigned long long p = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; p < pieces;
+       p += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint64_t e0 = p * LIST_PIECE, e1 = e0 + LIST_PIECE < entries ? e0 + LIST_PIECE : entries;
+    uint32_t lo = 0, hi = V;  // first vertex with off > e0, in (0, V]
+    while (lo < hi) {
+      const uint32_t mid = lo + ((hi - lo) >> 1);
+      if (off[mid] <= e0)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    for (uint32_t v = lo - 1; v < V && off[v] < e1; v++) {
+      const uint64_t a = off[v] > e0 ? off[v] : e0, b = off[v + 1] < e1 ? off[v + 1] : e1;
+      if (a < b) ds(v, VertexAdjList<E>(adj + a, adj + b));
+    }
+  }
+}
+
+// Dense slots: every message the signals emitted.
+template <typename R, typename M, class DL>
+__global__ void __launch_bounds__(THREADS)
+    list_dense_slot(const uint32_t *__restrict__ mv, const M *__restrict__ mm, unsigned n, DL dl, R *out) {
+  R r = R(0);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    r += dl(mv[i], mm[i]);
+  block_reduce_add(r, out);
+}
+
 struct OutDegree {
   const uint32_t *deg;
   __device__ unsigned long long operator()(uint32_t v) const { return deg[v]; }
@@ -448,11 +593,28 @@ class DeviceSubset {
     detail::fill_bits<<<detail::grid_for(words, sms_), detail::THREADS, 0, s_>>>(data, size, words);
     cuda_check(cudaGetLastError(), "subset fill");
   }
-  void set_bit(uint32_t v) {
+  // On the host: sets one bit with a kernel on the engine's stream.  In
+  // device code (callbacks of the list form): an atomic OR, as the
+  // reference's set_bit (core/bitmap.hpp:54-56).
+  __host__ __device__ void set_bit(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+    atomicOr(data + (v >> 6), 1ull << (v & 63));
+#else
     if (v >= size) throw Error(GG_ERR_INVALID, "set_bit: vertex out of range");
     detail::set_one_bit<<<1, 1, 0, s_>>>(data, v);
     cuda_check(cudaGetLastError(), "subset set_bit");
+#endif
   }
+  __device__ bool get_bit(uint32_t v) const { return (data[v >> 6] >> (v & 63)) & 1ull; }
+  // Subsets live in managed memory, so that a callback may dereference the
+  // pointer the reference's code holds (active_out->set_bit(dst)); delete
+  // frees them as the reference's toolkits do.
+  static void *operator new(size_t n) {
+    void *p = nullptr;
+    cuda_check(cudaMallocManaged(&p, n), "subset");
+    return p;
+  }
+  static void operator delete(void *p) { cudaFree(p); }
 
  private:
   cudaStream_t s_;
@@ -469,6 +631,30 @@ struct SubsetRef {
   }
 };
 inline SubsetRef ref(DeviceSubset *s) { return SubsetRef{s->data}; }
+
+// The graph as the list form's callbacks see it (Engine::device_graph(), in
+// managed memory): the reference's public fields and emit (core/graph.hpp:
+// 94-111, 1480-1490), which appends (vertex, message) to the current call's
+// message buffer.
+template <typename EdgeData>
+struct DeviceGraph {
+  VertexId vertices;
+  EdgeId edges;
+  int partition_id;
+  int partitions;
+  uint32_t *msg_v;
+  void *msg_m;
+  unsigned *msg_len;
+  unsigned msg_cap;
+  template <typename M>
+  __device__ void emit(VertexId v, M msg) const {
+    const unsigned i = atomicAdd(msg_len, 1u);
+    if (i < msg_cap) {
+      msg_v[i] = v;
+      static_cast<M *>(msg_m)[i] = msg;
+    }
+  }
+};
 
 template <typename EdgeData = Empty>
 class Engine {
@@ -492,9 +678,11 @@ class Engine {
   }
   ~Engine() {
     if (s_) cudaStreamSynchronize(s_);
-    void *ps[] = {red_, qlen_, qv_, qm_, pre_, tiles_, med_, heavy_, chunk_owner_, chunk_first_, partials_, dmsg_};
+    void *ps[] = {red_, qlen_, qv_, qm_, pre_, tiles_, med_, heavy_, chunk_owner_, chunk_first_, partials_, dmsg_,
+                  lmv_, lmm_, dgraph_};
     for (void *p : ps)
       if (p) cudaFree(p);
+    free_list_adjacency();
     if (s_) cudaStreamDestroy(s_);
   }
   Engine(const Engine &) = delete;
@@ -535,6 +723,91 @@ class Engine {
     graph_.transpose();
     refresh();
     build_bins();
+    free_list_adjacency();
+  }
+
+  // The graph handle for the list form's callbacks (allocated once, in
+  // managed memory).
+  DeviceGraph<EdgeData> *device_graph() {
+    if (!dgraph_) {
+      cuda_check(cudaMallocManaged(&dgraph_, sizeof(DeviceGraph<EdgeData>)), "device graph");
+      memset(dgraph_, 0, sizeof(DeviceGraph<EdgeData>));
+    }
+    auto *dg = static_cast<DeviceGraph<EdgeData> *>(dgraph_);
+    dg->vertices = vertices;
+    dg->edges = edges;
+    dg->partition_id = 0;
+    dg->partitions = 1;
+    return dg;
+  }
+
+  // core/graph.hpp:1493-1869, list form (see the top of this file): the
+  // callbacks take whole (pieces of) adjacency lists, as in the reference.
+  template <typename R, typename M, class SS, class SL, class DS, class DL>
+  R process_edges(SS sparse_signal, SL sparse_slot, DS dense_signal, DL dense_slot, DeviceSubset *active,
+                  DeviceSubset *dense_selective = nullptr) {
+    (void)dense_selective;
+    static_assert(std::is_arithmetic<R>::value, "process_edges reduces an arithmetic type");
+    static_assert(std::is_trivially_copyable<M>::value, "messages are stored in device buffers");
+    DeviceGraph<EdgeData> *dg = device_graph();
+    const unsigned long long active_edges = process_vertices<unsigned long long>(detail::OutDegree{out_degree}, active);
+    R *out = reinterpret_cast<R *>(red_);
+    cuda_check(cudaMemsetAsync(red_, 0, 16, s_), "process_edges");
+    cuda_check(cudaMemsetAsync(qlen_, 0, sizeof(unsigned), s_), "process_edges");
+    if (active_edges < edges / 20) {
+      last_mode = 0;
+      ensure_messages(sizeof(M));
+      AdjUnit<EdgeData> *adj = list_adjacency(false);
+      sync();
+      dg->msg_v = qv_;
+      dg->msg_m = qm_;
+      dg->msg_len = qlen_;
+      dg->msg_cap = vertices + 1;
+      detail::list_sparse_signal<SS><<<detail::grid_for(active->words, sms_), detail::THREADS, 0, s_>>>(
+          active->data, active->words, vertices, sparse_signal);
+      cuda_check(cudaGetLastError(), "sparse signal");
+      const unsigned n = messages_emitted(vertices + 1);
+      if (n) {
+        const size_t ntiles = ((size_t)n + detail::SCAN_TILE - 1) / detail::SCAN_TILE;
+        cuda_check(cudaMemsetAsync(tiles_, 0, sizeof(unsigned long long) * (ntiles + 1), s_), "scan");
+        detail::scan_tile_sums<<<(unsigned)ntiles, detail::THREADS, 0, s_>>>(qv_, out_degree, n, tiles_);
+        detail::scan_tiles_serial<<<1, 32, 0, s_>>>(tiles_, ntiles);
+        detail::scan_tile_apply<<<(unsigned)ntiles, detail::THREADS, 0, s_>>>(qv_, out_degree, n, tiles_, ntiles,
+                                                                             pre_);
+        unsigned long long total = 0;
+        cuda_check(cudaMemcpyAsync(&total, pre_ + n, sizeof(total), cudaMemcpyDeviceToHost, s_), "scan");
+        sync();
+        const unsigned long long pieces = (total + detail::LIST_PIECE - 1) / detail::LIST_PIECE;
+        if (pieces)
+          detail::list_sparse_slot<R, M, EdgeData, SL><<<detail::grid_for(pieces, sms_, 16), detail::THREADS, 0, s_>>>(
+              adj, out_.offsets, qv_, reinterpret_cast<const M *>(qm_), pre_, n, sparse_slot, out);
+        cuda_check(cudaGetLastError(), "sparse slot");
+      }
+    } else {
+      last_mode = 1;
+      const unsigned long long pieces = (in_.entries + detail::LIST_PIECE - 1) / detail::LIST_PIECE;
+      const size_t cap = (size_t)vertices + pieces + 1;
+      ensure_list_messages(cap, sizeof(M));
+      AdjUnit<EdgeData> *adj = list_adjacency(true);
+      sync();
+      dg->msg_v = lmv_;
+      dg->msg_m = lmm_;
+      dg->msg_len = qlen_;
+      dg->msg_cap = (unsigned)cap;
+      if (pieces)
+        detail::list_dense_signal<EdgeData, DS><<<detail::grid_for(pieces, sms_, 16), detail::THREADS, 0, s_>>>(
+            adj, in_.offsets, vertices, in_.entries, dense_signal);
+      cuda_check(cudaGetLastError(), "dense signal");
+      const unsigned n = messages_emitted((unsigned)cap);
+      if (n)
+        detail::list_dense_slot<R, M, DL><<<detail::grid_for(n, sms_), detail::THREADS, 0, s_>>>(
+            lmv_, reinterpret_cast<const M *>(lmm_), n, dense_slot, out);
+      cuda_check(cudaGetLastError(), "dense slot");
+    }
+    R r;
+    cuda_check(cudaMemcpyAsync(&r, out, sizeof(R), cudaMemcpyDeviceToHost, s_), "process_edges");
+    sync();
+    return r;
   }
 
   // core/graph.hpp:1406-1469
@@ -681,6 +954,52 @@ class Engine {
     cuda_check(cudaMalloc(&dmsg_, need), "dense messages");
     dmsg_bytes_ = need;
   }
+  // Messages the signals emitted; more than the buffer holds is an error
+  // (a signal emitted more than once per call).
+  unsigned messages_emitted(unsigned cap) {
+    unsigned n = 0;
+    cuda_check(cudaMemcpyAsync(&n, qlen_, sizeof(n), cudaMemcpyDeviceToHost, s_), "emit count");
+    sync();
+    if (n > cap) throw Error(GG_ERR_LIMIT, "process_edges: signals emitted more messages than one per call");
+    return n;
+  }
+  void ensure_list_messages(size_t cap, size_t msg_bytes) {
+    if (cap * msg_bytes <= lmm_bytes_ && cap * sizeof(uint32_t) <= lmv_bytes_) return;
+    sync();
+    if (lmv_) cudaFree(lmv_);
+    if (lmm_) cudaFree(lmm_);
+    cuda_check(cudaMalloc(&lmv_, cap * sizeof(uint32_t)), "dense messages");
+    cuda_check(cudaMalloc(&lmm_, cap * msg_bytes), "dense messages");
+    lmv_bytes_ = cap * sizeof(uint32_t);
+    lmm_bytes_ = cap * msg_bytes;
+  }
+  // The adjacency as AdjUnit entries: an unweighted entry is the neighbour id
+  // itself (the library's array, read in place); weighted entries are an
+  // interleaved copy made on first use.
+  AdjUnit<EdgeData> *list_adjacency(bool incoming) {
+    const gg_device_adj &d = incoming ? in_ : out_;
+    if constexpr (std::is_same<EdgeData, Empty>::value) {
+      static_assert(sizeof(AdjUnit<Empty>) == sizeof(uint32_t), "an unweighted entry is its neighbour id");
+      return reinterpret_cast<AdjUnit<Empty> *>(const_cast<uint32_t *>(d.neighbours));
+    } else {
+      AdjUnit<EdgeData> *&a = incoming ? adj_in_ : adj_out_;
+      AdjUnit<EdgeData> *other = incoming ? adj_out_ : adj_in_;
+      if (!a && other && in_.neighbours == out_.neighbours) a = other;  // symmetric: one copy
+      if (!a) {
+        if (!d.weights) throw Error(GG_ERR_UNWEIGHTED, "the list form needs the graph's edge data");
+        cuda_check(cudaMalloc(&a, sizeof(AdjUnit<EdgeData>) * (d.entries ? d.entries : 1)), "adjacency units");
+        detail::interleave_adjacency<EdgeData><<<detail::grid_for(d.entries, sms_), detail::THREADS, 0, s_>>>(
+            d.neighbours, d.weights, d.entries, a);
+        cuda_check(cudaGetLastError(), "adjacency units");
+      }
+      return a;
+    }
+  }
+  void free_list_adjacency() {
+    if (adj_out_) cudaFree(adj_out_);
+    if (adj_in_ && adj_in_ != adj_out_) cudaFree(adj_in_);
+    adj_out_ = adj_in_ = nullptr;
+  }
   void ensure_partials(size_t bytes) {
     if (bytes <= partial_bytes_) return;
     sync();
@@ -706,6 +1025,12 @@ class Engine {
   size_t partial_bytes_ = 0;
   void *dmsg_ = nullptr;
   size_t dmsg_bytes_ = 0;
+  // list form: dense messages, interleaved adjacency units, the device graph
+  uint32_t *lmv_ = nullptr;
+  void *lmm_ = nullptr;
+  size_t lmv_bytes_ = 0, lmm_bytes_ = 0;
+  AdjUnit<EdgeData> *adj_out_ = nullptr, *adj_in_ = nullptr;
+  void *dgraph_ = nullptr;
 };
 
 }  // namespace gemini

@@ -30,6 +30,38 @@ struct Empty {};
 typedef uint32_t VertexId;
 typedef uint64_t EdgeId;
 
+#if defined(__CUDACC__)
+#define GEMINI_HD __host__ __device__
+#else
+#define GEMINI_HD
+#endif
+
+// One adjacency entry and one vertex's adjacency list in the reference's
+// layout (core/type.hpp:44-68): neighbour id, then the edge data, packed; an
+// unweighted entry is the bare 4-byte id.  The list form of
+// gemini::Engine::process_edges (gemini/engine.cuh) hands callbacks these.
+template <typename EdgeData>
+struct AdjUnit {
+  VertexId neighbour;
+  EdgeData edge_data;
+} __attribute__((packed));
+
+template <>
+struct AdjUnit<Empty> {
+  union {
+    VertexId neighbour;
+    Empty edge_data;
+  };
+} __attribute__((packed));
+
+template <typename EdgeData>
+struct VertexAdjList {
+  AdjUnit<EdgeData> *begin;
+  AdjUnit<EdgeData> *end;
+  GEMINI_HD VertexAdjList() : begin(nullptr), end(nullptr) {}
+  GEMINI_HD VertexAdjList(AdjUnit<EdgeData> *b, AdjUnit<EdgeData> *e) : begin(b), end(e) {}
+};
+
 #define WORD_OFFSET(i) ((i) >> 6)
 #define BIT_OFFSET(i) ((i) & 0x3f)
 

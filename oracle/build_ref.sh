@@ -63,4 +63,25 @@ for app in bfs cc pagerank sssp bc; do
   pids+=($!)
 done
 for p in "${pids[@]}"; do wait "$p"; done
+# The reference's SSSP callbacks on this library's engine (ref_engine_sssp.cu):
+# the four process_edges callbacks of toolkits/sssp.cpp, each lambda made a
+# by-value __device__ lambda, compiled against gemini/engine.cuh.  Needs nvcc
+# and the library (built first by __graft_entry__.build()).
+REPO="$(cd "$HERE/.." && pwd)"
+LIB="$REPO/geminigraph_gb300/libgemini_gb300.so"
+NVCC="${NVCC:-/usr/local/cuda/bin/nvcc}"
+INC="$SRC/sssp_callbacks.inc"
+awk '/graph->process_edges<VertexId,Weight>\(/ {on = 1; next} on && /^[[:space:]]*active_in[[:space:]]*$/ {exit} on {print}' \
+  "$SRC/toolkits/sssp.cpp" | sed 's/\[&\](/[=] __device__ (/g' > "$INC.tmp"
+if ! cmp -s "$INC.tmp" "$INC"; then mv "$INC.tmp" "$INC"; else rm -f "$INC.tmp"; fi
+if [ -x "$NVCC" ] && [ -f "$LIB" ] && [ -s "$INC" ]; then
+  if ! [ "$BIN/ref_engine_sssp" -nt "$HERE/ref_engine_sssp.cu" ] || ! [ "$BIN/ref_engine_sssp" -nt "$INC" ] ||
+     ! [ "$BIN/ref_engine_sssp" -nt "$REPO/geminigraph_gb300/cpp/gemini/engine.cuh" ] ||
+     ! [ "$BIN/ref_engine_sssp" -nt "$LIB" ]; then
+    "$NVCC" -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 --extended-lambda \
+      -I"$REPO/include" -I"$REPO/geminigraph_gb300/cpp" -I"$SRC" "$HERE/ref_engine_sssp.cu" \
+      -o "$BIN/ref_engine_sssp" -L"$REPO/geminigraph_gb300" -lgemini_gb300 \
+      -Xlinker -rpath,'$ORIGIN/../../../geminigraph_gb300'
+  fi
+fi
 echo "build_ref: toolkits in $BIN"

@@ -121,3 +121,25 @@ def test_engine_bc(graph, tmp_path):
     fin = np.isfinite(oinv)
     assert rel_l1(inv[fin], oinv[fin]) < TOL
     assert modes == [m for m, _, _ in otrace]
+
+
+REF_SSSP = os.path.join(REPO, "oracle", "_ref", "bin", "ref_engine_sssp")
+
+
+def test_reference_sssp_callbacks_on_the_engine(graph, tmp_path):
+    """The reference's own SSSP callbacks (toolkits/sssp.cpp:46-80, each
+    lambda only made a by-value __device__ lambda; oracle/build_ref.sh)
+    through the engine's list form of process_edges: distances bit-exact and
+    every call in the oracle's mode.  The slots' returns count messages that
+    lowered a distance, as the reference's do, so they are not compared."""
+    if not os.path.exists(REF_SSSP):
+        pytest.skip("reference sources not staged here (oracle/build_ref.sh)")
+    V, s, d, w, root, _, pw = graph
+    out = str(tmp_path / "ref_sssp.out")
+    p = subprocess.run([REF_SSSP, pw, str(V), str(root), out], capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr
+    modes = [int(line.split()[3]) for line in p.stdout.splitlines() if line.startswith("call ")]
+    dist = np.fromfile(out, dtype=np.float32)
+    odist, otrace = OracleGraph(V, s, d, w).sssp(root)
+    assert np.array_equal(dist.view(np.uint32), odist.view(np.uint32))
+    assert modes == [m for m, _, _ in otrace]

@@ -14,11 +14,15 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libgemini_gb300.so")
+# GG_LIBRARY=check selects libgemini_gb300_check.so, the build with device
+# bounds checks (a failed check makes the call return GG_ERR_CHECK)
+LIB_PATH = os.path.join(PKG, "libgemini_gb300_check.so" if os.environ.get("GG_LIBRARY") == "check"
+                        else "libgemini_gb300.so")
 
 GG_OK = 0
 STATUS = {1: "invalid argument", 2: "I/O error", 3: "vertex id out of range", 4: "CUDA error",
-          5: "out of memory", 6: "graph is unweighted", 7: "graph too large", 8: "capacity exceeded"}
+          5: "out of memory", 6: "graph is unweighted", 7: "graph too large", 8: "capacity exceeded",
+          9: "device bounds check failed"}
 
 RMAT, GRID = 0, 1
 

@@ -32,8 +32,16 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build_library(verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+LIB_CHECK = os.path.join(PKG, "libgemini_gb300_check.so")
+
+
+def build_library(verbose=False, check=False):
+    """check=True builds libgemini_gb300_check.so: the same library with the
+    device bounds checks of GG_CHECK compiled in (gg_common.cuh)."""
+    build_dir = BUILD + ("_check" if check else "")
+    lib = LIB_CHECK if check else LIB
+    flags = NVCC_FLAGS + (["-DGG_CHECK"] if check else [])
+    os.makedirs(build_dir, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
         glob.glob(os.path.join(INCLUDE, "*.h"))
@@ -41,10 +49,10 @@ def build_library(verbose=False):
     objs = []
     jobs = []
     for src in sources:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc] + flags + ["-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -58,9 +66,9 @@ def build_library(verbose=False):
         for err in ex.map(run, jobs):
             if verbose and err:
                 print(err)
-    if _stale(LIB, objs):
-        run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
-    return LIB
+    if _stale(lib, objs):
+        run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lpthread"])
+    return lib
 
 
 CPP = os.path.join(PKG, "cpp")
@@ -120,8 +128,9 @@ def build_examples(verbose=False):
 
 def build(verbose=False):
     lib = build_library(verbose)
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        jobs = [ex.submit(build_toolkits, verbose), ex.submit(build_examples, verbose)]
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        jobs = [ex.submit(build_toolkits, verbose), ex.submit(build_examples, verbose),
+                ex.submit(build_library, verbose, True)]
         for j in jobs:
             j.result()
     return lib

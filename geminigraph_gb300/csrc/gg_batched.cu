@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256)
           uint32_t u[4];
           u64 f[4];
 #pragma unroll
-          for (int i = 0; i < 4; i++) u[i] = k + i < e ? d.nbr[k + i] : 0u;
+          for (int i = 0; i < 4; i++) u[i] = k + i < e ? nbr_at(d, k + i, GG_SITE) : 0u;
 #pragma unroll
           for (int i = 0; i < 4; i++) f[i] = k + i < e ? front[u[i]] : 0ull;
 #pragma unroll
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(256)
       u64 m = 0;
       uint32_t u = 0;
       if (k < e) {
-        u = d.nbr[k];
+        u = nbr_at(d, k, GG_SITE);
         m = front[u] & need;
       }
       if (m) {
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
       if (e < e1) {
         const uint32_t i = upper_bound_idx<unsigned long long>(P, lo, hi, e) - 1;
         const uint32_t u = q[i];
-        v = d.nbr[d.off[u] + (e - P[i])];
+        v = nbr_at(d, d.off[u] + (e - P[i]), GG_SITE);
         const u64 m = front[u] & ~visit[v];
         if (m && (m & ~*(volatile u64 *)(next + v))) {
           const u64 old = atomicOr(next + v, m);
@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
         u = q[i];
         k = d.off[u] + (e - P[i]);
       }
-      const uint32_t v = d.nbr[k];
+      const uint32_t v = nbr_at(d, k, GG_SITE);
       const float wt = d.w[k];
       const u64 fm = front[u];
       bool low0 = false, low1 = false;
@@ -746,7 +746,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
         u = q[i];
         k = d.off[u] + (e - P[i]);
       }
-      const uint32_t v = d.nbr[k];
+      const uint32_t v = nbr_at(d, k, GG_SITE);
       const float wt = d.w[k];
       u64 fm = front[u], low = 0;
       while (fm) {

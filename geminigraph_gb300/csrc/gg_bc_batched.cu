@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256)
         hi = mid;
     }
     const uint32_t i = lo - 1, u = q[i];
-    const uint32_t v = d.nbr[d.off[u] + (e - prefix[i])];
+    const uint32_t v = nbr_at(d, d.off[u] + (e - prefix[i]), GG_SITE);
     u64 m = front[u] & ~visit[v];
     if (!m) continue;
     atomicOr(next + v, m);
@@ -126,7 +126,7 @@ __device__ __forceinline__ u64 warp_gather_paths(const Dir &d, u64 b, u64 e, u64
     uint32_t u = 0;
     u64 f = 0;
     if (k < e) {
-      u = d.nbr[k];
+      u = nbr_at(d, k, GG_SITE);
       f = front[u] & need;
     }
     unsigned bal = __ballot_sync(GG_FULL, f != 0);
@@ -219,7 +219,7 @@ __device__ __forceinline__ void warp_gather_dep(const Dir &d, u64 b, u64 e, u64 
     uint32_t w = 0;
     u64 f = 0;
     if (k < e) {
-      w = d.nbr[k];
+      w = nbr_at(d, k, GG_SITE);
       f = nxt[w] & m;
     }
     unsigned bal = __ballot_sync(GG_FULL, f != 0);

@@ -21,6 +21,7 @@
 #include <stdio.h>
 
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/gemini_gb300.h"
@@ -77,6 +78,10 @@ struct Dir {
   uint32_t *big_chunk = nullptr;    // nbig+1: prefix of per-vertex chunk counts (aligned blocks, see big_range)
   uint32_t *big_owner = nullptr;    // nbigchunks: index into big of each chunk
   uint32_t nbigchunks = 0;
+  // bounds of the ids and entries, and the graph's error word (GG_CHECK builds)
+  uint32_t nv = 0;
+  uint64_t ne = 0;
+  unsigned *err = nullptr;
 };
 
 // Per-call counters written by the activation epilogue of every edge kernel.
@@ -191,6 +196,9 @@ struct gg_graph {
   // reduction pulls on the hot-source layout: gathered state of the first
   // l1_hot_bytes worth of sources is cached in L1, the rest read past it
   uint32_t l1_hot_bytes = 0xffffffffu;
+  // device error word of the bounds checks of a GG_CHECK build: first
+  // failing site, its value (low, high), number of failures
+  unsigned *check_err = nullptr;
   // CC and SSSP: a dense call (by the reference's switch) whose active
   // out-edges are below nadj / dense_push_div runs the push kernels over the
   // frontier instead of pulling every in-list (0: always pull; 4 measured
@@ -314,6 +322,7 @@ struct Trace {
   int collect();  // after the stream has been synchronised
 };
 
+int check_status(gg_graph *g);
 int timed_begin(gg_graph *g);
 int timed_end(gg_graph *g, gg_run_stats *st, int launches);
 
@@ -345,6 +354,64 @@ __device__ __forceinline__ void big_range(const Dir &d, uint32_t c, uint32_t chu
   *lo = (b0 / chunk + (c - d.big_chunk[o])) * (unsigned long long)chunk;
   *b = b0 > *lo ? b0 : *lo;
   *e = e0 < *lo + chunk ? e0 : *lo + chunk;
+}
+
+// ---------------------------------------------------------------- bounds checks
+// A GG_CHECK build (libgemini_gb300_check.so) checks every adjacency entry
+// index against the direction's entries and every neighbour id read from the
+// adjacency against the vertex count before it is used.  A failing check
+// records its site (16-bit hash of the source file name, line) and value in
+// the graph's error word, substitutes 0 so that no access leaves its array,
+// and the run returns GG_ERR_CHECK.  Other builds compile the plain loads.
+constexpr uint32_t site_file_hash(const char *f) {
+  const char *b = f;
+  for (const char *p = f; *p; p++)
+    if (*p == '/') b = p + 1;
+  uint32_t h = 2166136261u;
+  for (const char *p = b; *p; p++) h = (h ^ (uint32_t)(unsigned char)*p) * 16777619u;
+  return (h ^ (h >> 16)) & 0xffffu;
+}
+#define GG_SITE \
+  (std::integral_constant<uint32_t, (gg::site_file_hash(__FILE__) << 16) | ((uint32_t)__LINE__ & 0xffffu)>::value)
+
+__device__ __forceinline__ void check_fail(unsigned *err, uint32_t site, unsigned long long value) {
+  if (!err) return;
+  if (atomicCAS(err, 0u, site) == 0u) {
+    err[1] = (unsigned)value;
+    err[2] = (unsigned)(value >> 32);
+  }
+  atomicAdd(err + 3, 1u);
+}
+// The neighbour id of entry k of direction d.
+__device__ __forceinline__ uint32_t nbr_at(const Dir &d, unsigned long long k, uint32_t site) {
+#if defined(GG_CHECK)
+  if (k >= d.ne) {
+    check_fail(d.err, site, k);
+    return 0u;
+  }
+  const uint32_t u = d.nbr[k];
+  if (u >= d.nv) {
+    check_fail(d.err, site, u);
+    return 0u;
+  }
+  return u;
+#else
+  (void)site;
+  return d.nbr[k];
+#endif
+}
+// A vertex id loaded some other way (vector loads, queues).
+__device__ __forceinline__ uint32_t vertex_ok(const Dir &d, uint32_t u, uint32_t site) {
+#if defined(GG_CHECK)
+  if (u >= d.nv) {
+    check_fail(d.err, site, u);
+    return 0u;
+  }
+#else
+  (void)d;
+  (void)site;
+#endif
+  return u;
 }
 
 // Adjacency entries that a warp reads once (coalesced) are not kept in L1,
@@ -379,6 +446,19 @@ __device__ __forceinline__ double ld_once(const double *p) {
 template <typename T>
 __device__ __forceinline__ T ld_gather(const T *a, uint32_t u, uint32_t hot) {
   return u < hot ? a[u] : ld_once(a + u);
+}
+// nbr_at for entries a warp reads once (past L1).
+__device__ __forceinline__ uint32_t nbr_once(const Dir &d, unsigned long long k, uint32_t site) {
+#if defined(GG_CHECK)
+  if (k >= d.ne) {
+    check_fail(d.err, site, k);
+    return 0u;
+  }
+  return vertex_ok(d, ld_once(d.nbr + k), site);
+#else
+  (void)site;
+  return ld_once(d.nbr + k);
+#endif
 }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 

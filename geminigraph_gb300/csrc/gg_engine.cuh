@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(PUSH_THREADS)
           src = q[qi];
           k = d.off[src] + (e - P[qi]);
         }
-        dst = d.nbr[k];
+        dst = nbr_at(d, k, GG_SITE);
         float w = d.w ? d.w[k] : 0.0f;
         pred = op.push(src, qi, dst, w);
       }
@@ -214,12 +214,12 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
       Acc acc = op.identity(v);
       unsigned long long k = b;
       for (; k + 4 <= e; k += 4) {
-        const uint32_t u0 = d.nbr[k], u1 = d.nbr[k + 1], u2 = d.nbr[k + 2], u3 = d.nbr[k + 3];
+        const uint32_t u0 = nbr_at(d, k, GG_SITE), u1 = nbr_at(d, k + 1, GG_SITE), u2 = nbr_at(d, k + 2, GG_SITE), u3 = nbr_at(d, k + 3, GG_SITE);
         Acc g0 = op.gather(d, k, u0), g1 = op.gather(d, k + 1, u1), g2 = op.gather(d, k + 2, u2),
             g3 = op.gather(d, k + 3, u3);
         acc = op.combine(op.combine(op.combine(op.combine(acc, g0), g1), g2), g3);
       }
-      for (; k < e; k++) acc = op.combine(acc, op.gather(d, k, d.nbr[k]));
+      for (; k < e; k++) acc = op.combine(acc, op.gather(d, k, nbr_at(d, k, GG_SITE)));
       a = op.finish(v, acc, deg, t);
     }
     if (act.active_out) pull_activate(a, v, g, act, t);
@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(PULL_THREADS)
 #pragma unroll
         for (int i = 0; i < WIN; i++) {
           const unsigned long long p = lo + 4 * (lane + 32 * i);
-          const uint32_t u[4] = {w[i].x, w[i].y, w[i].z, w[i].w};
+          const uint32_t u[4] = {vertex_ok(d, w[i].x, GG_SITE), vertex_ok(d, w[i].y, GG_SITE),
+                                 vertex_ok(d, w[i].z, GG_SITE), vertex_ok(d, w[i].w, GG_SITE)};
 #pragma unroll
           for (int j = 0; j < 4; j++) {
             const bool in = p + j >= b && p + j < e;
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(PULL_THREADS)
 #pragma unroll
         for (int j = 0; j < PER_LANE; j++) {
           const unsigned long long k = b + lane + 32 * j;
-          u[j] = k < e ? ld_once(d.nbr + k) : 0u;
+          u[j] = k < e ? nbr_once(d, k, GG_SITE) : 0u;
           if constexpr (WT) wt[j] = k < e ? ld_once(d.w + k) : 0.0f;
         }
 #pragma unroll
@@ -391,10 +392,10 @@ static __global__ void __launch_bounds__(PULL_THREADS, 8)
     if (todo) {
       unsigned long long lim = e - b <= d.light ? e : b + d.light;
       for (unsigned long long k = b; k < lim && found == NONE32; k += 4) {
-        uint32_t s0 = d.nbr[k];
-        uint32_t s1 = k + 1 < lim ? d.nbr[k + 1] : s0;
-        uint32_t s2 = k + 2 < lim ? d.nbr[k + 2] : s0;
-        uint32_t s3 = k + 3 < lim ? d.nbr[k + 3] : s0;
+        uint32_t s0 = nbr_at(d, k, GG_SITE);
+        uint32_t s1 = k + 1 < lim ? nbr_at(d, k + 1, GG_SITE) : s0;
+        uint32_t s2 = k + 2 < lim ? nbr_at(d, k + 2, GG_SITE) : s0;
+        uint32_t s3 = k + 3 < lim ? nbr_at(d, k + 3, GG_SITE) : s0;
         bool h0 = bm_test_ldg(active_in, s0), h1 = bm_test_ldg(active_in, s1);
         bool h2 = bm_test_ldg(active_in, s2), h3 = bm_test_ldg(active_in, s3);
         found = h0 ? s0 : h1 ? s1 : h2 ? s2 : h3 ? s3 : NONE32;
@@ -437,7 +438,7 @@ static __global__ void __launch_bounds__(PULL_THREADS)
         uint32_t s = 0;
         bool hit = false;
         if (k < e) {
-          s = d.nbr[k];
+          s = nbr_at(d, k, GG_SITE);
           hit = bm_test_ldg(active_in, s);
         }
         unsigned m = __ballot_sync(GG_FULL, hit);
@@ -475,7 +476,7 @@ static __global__ void __launch_bounds__(PULL_THREADS)
       if (lane == 0) best = *(volatile unsigned long long *)(first + h);
       if (__shfl_sync(GG_FULL, best, 0) < base) break;
       const unsigned long long k = base + lane;
-      const bool hit = k < e && bm_test_ldg(active_in, d.nbr[k]);
+      const bool hit = k < e && bm_test_ldg(active_in, nbr_at(d, k, GG_SITE));
       const unsigned bal = __ballot_sync(GG_FULL, hit);
       if (bal) {
         if (lane == 0) atomicMin(first + h, base + (unsigned long long)(__ffs(bal) - 1));
@@ -497,7 +498,7 @@ static __global__ void __launch_bounds__(PULL_THREADS)
       v = d.heavy[h];
       const unsigned long long f = first[h];
       if (f != ~0ull && !bm_test(act.visited, v)) {
-        parent[v] = d.nbr[f];
+        parent[v] = nbr_at(d, f, GG_SITE);
         a = true;
       }
     }
@@ -588,7 +589,7 @@ __device__ __forceinline__ void small_call(SmallRun *st, const uint32_t *__restr
     }
     if (valid && e - b <= LIGHT_DEG) {
       for (unsigned long long k = b; k < e; k++) {
-        uint32_t dst = d.nbr[k];
+        uint32_t dst = nbr_at(d, k, GG_SITE);
         if (op.push(src, (uint32_t)i, dst, d.w ? d.w[k] : 0.0f))
           small_activate<kUnique>(dst, st, stamp, level, visited, q_out, out_deg, in_deg, t);
       }
@@ -601,7 +602,7 @@ __device__ __forceinline__ void small_call(SmallRun *st, const uint32_t *__restr
       const uint32_t lsrc = __shfl_sync(GG_FULL, src, leader);
       const uint32_t li = (uint32_t)__shfl_sync(GG_FULL, (unsigned long long)i, leader);
       for (unsigned long long k = lb + lane; k < le; k += 32) {
-        uint32_t dst = d.nbr[k];
+        uint32_t dst = nbr_at(d, k, GG_SITE);
         if (op.push(lsrc, li, dst, d.w ? d.w[k] : 0.0f))
           small_activate<kUnique>(dst, st, stamp, level, visited, q_out, out_deg, in_deg, t);
       }
@@ -647,7 +648,7 @@ __device__ __forceinline__ void small_call_t(Counters *tally, const uint32_t *__
     }
     if (valid && e - b <= LIGHT_DEG) {
       for (unsigned long long k = b; k < e; k++) {
-        uint32_t dst = d.nbr[k];
+        uint32_t dst = nbr_at(d, k, GG_SITE);
         if (op.push(src, (uint32_t)i, dst, d.w ? d.w[k] : 0.0f))
           small_activate_t<kUnique>(dst, tally, stamp, level, visited, q_out, out_deg, in_deg, t);
       }
@@ -660,7 +661,7 @@ __device__ __forceinline__ void small_call_t(Counters *tally, const uint32_t *__
       const uint32_t lsrc = __shfl_sync(GG_FULL, src, leader);
       const uint32_t li = (uint32_t)__shfl_sync(GG_FULL, (unsigned long long)i, leader);
       for (unsigned long long k = lb + lane; k < le; k += 32) {
-        uint32_t dst = d.nbr[k];
+        uint32_t dst = nbr_at(d, k, GG_SITE);
         if (op.push(lsrc, li, dst, d.w ? d.w[k] : 0.0f))
           small_activate_t<kUnique>(dst, tally, stamp, level, visited, q_out, out_deg, in_deg, t);
       }

@@ -155,6 +155,28 @@ int Trace::collect() {
   return GG_OK;
 }
 
+// GG_CHECK builds: the run's bounds checks, read once it has finished.
+int check_status(gg_graph *g) {
+#if defined(GG_CHECK)
+  static const char *const files[] = {"gg_engine.cuh", "gg_common.cuh", "gg_batched.cu", "gg_bc_batched.cu",
+                                      "gg_store.cu",   "gg_bfs_pr.cu",  "gg_cc_sssp_bc.cu", "gg_partition.cu"};
+  unsigned h[4] = {0, 0, 0, 0};
+  GG_CUDA(cudaMemcpy(h, g->check_err, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h[0]) {
+    const char *file = "?";
+    for (const char *f : files)
+      if (site_file_hash(f) == (h[0] >> 16)) file = f;
+    GG_CUDA(cudaMemset(g->check_err, 0, sizeof(h)));
+    set_error("device bounds check failed at %s:%u: index or vertex id %llu out of range (%u failures)", file,
+              h[0] & 0xffffu, ((unsigned long long)h[2] << 32) | h[1], h[3]);
+    return GG_ERR_CHECK;
+  }
+#else
+  (void)g;
+#endif
+  return GG_OK;
+}
+
 int timed_begin(gg_graph *g) {
   GG_CUDA(cudaEventRecord(g->ev0, g->stream));
   return GG_OK;
@@ -163,6 +185,7 @@ int timed_begin(gg_graph *g) {
 int timed_end(gg_graph *g, gg_run_stats *st, int launches) {
   GG_CUDA(cudaEventRecord(g->ev1, g->stream));
   GG_CUDA(cudaEventSynchronize(g->ev1));
+  GG_TRY(check_status(g));
   float ms = 0;
   GG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
   if (st) {
@@ -573,6 +596,9 @@ static void adj_release(bool host, void *p) {
 // direction whose offsets are written.
 int finish_dir(gg_graph *g, Dir *d) {
   const uint32_t V = g->V;
+  d->nv = V;
+  d->ne = g->nadj;
+  d->err = g->check_err;
   degrees_from_offsets<<<grid_for(V, 256, g->num_sms, 16), 256, 0, g->stream>>>(d->off, V, d->deg);
   GG_CUDA(cudaGetLastError());
   size_t words = bitmap_words32(V);
@@ -665,7 +691,7 @@ __global__ void rank_edge_keys_light(Dir d, uint32_t V, int bits, const uint32_t
     const uint64_t b = d.off[v], e = d.off[v + 1];
     if (e - b > d.light) continue;
     const uint64_t hi = (uint64_t)rank_of[v] << bits;
-    for (uint64_t k = b; k < e; k++) keys[k] = hi | rank_of[d.nbr[k]];
+    for (uint64_t k = b; k < e; k++) keys[k] = hi | rank_of[nbr_at(d, k, GG_SITE)];
   }
 }
 
@@ -677,7 +703,7 @@ __global__ void rank_edge_keys_big(Dir d, int bits, const uint32_t *__restrict__
     unsigned long long lo, b, e;
     big_range(d, (uint32_t)c, d.chunk, &v, &lo, &b, &e);
     const uint64_t hi = (uint64_t)rank_of[v] << bits;
-    for (unsigned long long k = b + lane_id(); k < e; k += 32) keys[k] = hi | rank_of[d.nbr[k]];
+    for (unsigned long long k = b + lane_id(); k < e; k += 32) keys[k] = hi | rank_of[nbr_at(d, k, GG_SITE)];
   }
 }
 
@@ -830,6 +856,7 @@ void graph_destroy(gg_graph *g) {
     cudaStreamDestroy(g->side);
   }
   for (cudaEvent_t e : g->evpool) cudaEventDestroy(e);
+  if (g->check_err) cudaFree(g->check_err);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
 }
@@ -858,6 +885,8 @@ static int graph_create(int device, uint32_t V, int weighted, int symmetric, gg_
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaMalloc(&g->check_err, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(g->check_err, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&g->ws.ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMallocHost(&g->ws.ctr_host, sizeof(Counters));
   if (e == cudaSuccess) e = cudaHostAlloc(&g->ws.stage, STAGE_BYTES_HOST, cudaHostAllocMapped);

@@ -37,6 +37,7 @@ extern "C" {
 #define GG_ERR_UNWEIGHTED 6   /* the operation needs edge weights */
 #define GG_ERR_TOO_LARGE 7    /* adjacency entries per direction >= 2^32 */
 #define GG_ERR_LIMIT 8        /* a fixed capacity of the call was exceeded */
+#define GG_ERR_CHECK 9        /* a device bounds check failed (libgemini_gb300_check.so only) */
 
 typedef struct gg_graph gg_graph;
 

@@ -31,6 +31,18 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_checked_library_exports_the_same_symbols():
+    """libgemini_gb300_check.so (device bounds checks) is a drop-in for the
+    plain library."""
+    import ctypes
+    path = os.path.join(REPO, "geminigraph_gb300", "libgemini_gb300_check.so")
+    if not os.path.exists(path):
+        pytest.skip("checked library not built")
+    C = ctypes.CDLL(path)
+    missing = [n for n in declared_functions() if not hasattr(C, n)]
+    assert not missing, missing
+
+
 @pytest.mark.parametrize("kind,p1,p2,seed,weighted", [
     (gg.RMAT, 8, 16, 1, False), (gg.RMAT, 11, 16, 5, True), (gg.RMAT, 14, 4, 99, True),
     (gg.GRID, 2, 0, 0, False), (gg.GRID, 17, 0, 3, True), (gg.GRID, 64, 0, 5, False)])

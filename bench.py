@@ -401,6 +401,53 @@ def cpu_reference(workload, nsteps, warmup, first_root=0):
                 times=t, edges=e)
 
 
+def check_against_oracle(g, workload, arg):
+    """Checks one run of the timed workload, on its full-size graph, against
+    the oracle (bench.py --check; outside every timed region): BFS levels and
+    tree edges, CC labels and SSSP distances bit-exact, float PageRank within
+    1e-5 relative L1 of the oracle's double ranks, BC within 1e-10."""
+    from oracle import oracle
+    w = WORKLOADS[workload]
+    t0 = time.perf_counter()
+    kind = oracle.RMAT if w["kind"] == "rmat" else oracle.GRID
+    V = (1 << w["scale"]) if kind == oracle.RMAT else w["scale"] * w["scale"]
+    rec = oracle.records(kind, w["scale"], w["ef"], SEED, w["weighted"], threads=os.cpu_count() or 1)
+    rec = rec.reshape(-1, 3 if w["weighted"] else 2)
+    og = oracle.OracleGraph(V, rec[:, 0].copy(), rec[:, 1].copy(),
+                            rec[:, 2].copy().view(np.float32) if w["weighted"] else None, symmetric=w["symmetric"])
+    del rec
+
+    def rel(a, b):
+        return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+    out = {"workload": workload, "arg": arg}
+    if workload in ("bfs", "bfs_grid"):
+        parent, _ = g.bfs(arg)
+        oparent, otrace = og.bfs(arg)
+        out["levels_equal"] = bool(np.array_equal(oracle.tree_levels(parent, arg), oracle.tree_levels(oparent, arg)))
+        out["bad_tree_edges"] = og.tree_bad_edges(parent, arg)
+        out["passed"] = out["levels_equal"] and out["bad_tree_edges"] == 0
+    elif workload in ("pagerank", "pagerank_f64"):
+        ranks, _, _ = g.pagerank(arg, f32=workload == "pagerank")
+        oranks = og.pagerank(arg)[0]
+        out["rel_l1_vs_fp64"] = rel(ranks.astype(np.float64), oranks)
+        out["passed"] = out["rel_l1_vs_fp64"] < (1e-5 if workload == "pagerank" else 1e-10)
+    elif workload == "sssp":
+        dist, _ = g.sssp(arg)
+        out["passed"] = bool(np.array_equal(dist.view(np.uint32), og.sssp(arg)[0].view(np.uint32)))
+    elif workload == "cc":
+        label, _ = g.cc()
+        out["passed"] = bool(np.array_equal(label, og.cc()[0]))
+    else:
+        dep, _, _ = g.bc(arg)
+        odep = og.bc(arg)[0]
+        ok = ~np.isnan(odep)
+        out["rel_l1"] = rel(dep[ok], odep[ok])
+        out["passed"] = bool(np.array_equal(np.isnan(dep), np.isnan(odep))) and out["rel_l1"] < 1e-10
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
 def _boot_id():
     try:
         return open("/proc/sys/kernel/random/boot_id").read().strip()
@@ -626,6 +673,8 @@ def gpu_arm(args, dist):
                                     "frac": round(adj_rate / link, 4),
                                     "bytes": "adjacency bytes of the counted edges (pull-mode BFS reads fewer)",
                                     "peak_source": "measured pinned host->device copy (torch, CUDA events)"}
+    if args.check and dist.rank == 0:
+        line["check"] = check_against_oracle(g, args.workload, step_in[args.warmup])
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         try:
             r = cached_reference_result(args.workload)
@@ -1052,6 +1101,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bfs", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--check", action="store_true",
+                    help="after timing, check the first timed run against the oracle on the full-size graph")
     ap.add_argument("--bins", default="autotune", choices=["autotune", "default"],
                     help="degree bins: the autotuner's pick for this graph, or the library defaults")
     ap.add_argument("--scale", type=int, default=None, help="override the workload's R-MAT scale / grid side")

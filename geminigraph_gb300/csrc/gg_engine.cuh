@@ -186,12 +186,12 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 //   pull_light   one warp per 32 consecutive vertices, each lane serially
 //                over a list of <= d.light entries (and every deg-0 vertex);
 //                the warp owns the bitmap word of its 32 vertices
-//   pull_chunks / pull_big_finish
+//   pull_chunks / pull_big_finish(_warps)
 //                every longer list cut into d.chunk-edge chunks, one warp
-//                per chunk, then one lane per vertex combining its chunks in
-//                order
-// The chunk kernels run after pull_light in the same stream and set their
-// bitmap bits atomically.
+//                per chunk, then a lane (or, without activations, a warp)
+//                per vertex combining its chunks
+// The chunk kernel runs beside pull_light (second stream); the finish runs
+// after both and sets its bitmap bits atomically.
 template <class Op>
 __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op op, ActOut act, Counters *ctr) {
   using Acc = typename Op::Acc;
@@ -301,6 +301,32 @@ __global__ void __launch_bounds__(PULL_THREADS)
     part = op.warp_combine(part);
     if (lane == 0) partials[c] = part;
   }
+}
+
+// Long-list vertices of a call that activates nothing (PageRank, BC's
+// backward sweep): one warp per vertex; the lanes read its chunk partials
+// (coalesced, lane-strided), the warp tree combines them, lane 0 applies the
+// slot.  Measured against the lane-per-vertex finish below: PageRank R-MAT 20
+// 286 -> 326 GTEPS (there the lanes, adding up to 32 partials each in series,
+// are latency-bound); calls with activations keep the lane form, which
+// records a warp's 32 activations together (SSSP R-MAT 25: 145 against 138).
+template <class Op>
+__global__ void __launch_bounds__(PULL_THREADS)
+    pull_big_finish_warps(Dir d, Op op, const typename Op::Acc *__restrict__ partials, Counters *ctr) {
+  using Acc = typename Op::Acc;
+  Tally t;
+  const size_t nwarps = (size_t)gridDim.x * (PULL_THREADS / 32);
+  const unsigned lane = lane_id();
+  for (size_t i = (size_t)blockIdx.x * (PULL_THREADS / 32) + (threadIdx.x >> 5); i < d.nbig; i += nwarps) {
+    const uint32_t v = d.big[i];
+    if (!op.want(v)) continue;
+    const uint32_t c0 = d.big_chunk[i], c1 = d.big_chunk[i + 1];
+    Acc part = op.identity_coop();
+    for (uint32_t c = c0 + lane; c < c1; c += 32) part = op.combine(part, partials[c]);
+    part = op.warp_combine(part);
+    if (lane == 0) op.finish(v, op.combine(op.identity(v), part), d.deg[v], t);
+  }
+  t.flush(ctr);
 }
 
 // One lane per long-list vertex combines its chunk partials in order (a warp
@@ -917,8 +943,12 @@ struct Launch {
           pull_chunks<Op, 8, false><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
       }
       if (fork) GG_CUDA(cudaStreamWaitEvent(s, g->join, 0));
-      pull_big_finish<Op><<<grid_for(d.nbig, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, op, part, act,
-                                                                                                  ctr);
+      if (act.active_out)
+        pull_big_finish<Op><<<grid_for(d.nbig, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(d, op, part, act,
+                                                                                                    ctr);
+      else
+        pull_big_finish_warps<Op><<<grid_for((size_t)d.nbig * 32, PULL_THREADS, g->num_sms, 8), PULL_THREADS, 0, s>>>(
+            d, op, part, ctr);
       launches += 2;
     }
     GG_CUDA(cudaGetLastError());

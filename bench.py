@@ -534,7 +534,8 @@ def tune_bins(g, args):
     """Degree bins for this graph: the library defaults, or the autotuner's
     pick for the workload's kernels (timed on the graph, cached on disk)."""
     if args.bins == "default":
-        return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1, "l1_hot_bytes": None}
+        return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1, "l1_hot_bytes": None,
+                "pull_split": 0}
     objective = ("pagerank",) if args.workload.startswith("pagerank") else \
         ("batched",) if args.workload in ("bfs_batched", "sssp_batched", "bc_batched", "serve") else \
         ("bfs",) if args.workload.startswith("bfs") else ("sssp",) if args.workload == "sssp" else \
@@ -544,7 +545,7 @@ def tune_bins(g, args):
     return {"source": "autotune(%s)" % "+".join(objective), "light_deg": r["light_deg"],
             "pull_chunk": r["pull_chunk"], "pull_vector": r["pull_vector"],
             "l1_hot_bytes": None if r["l1_hot_bytes"] == 0xffffffff else r["l1_hot_bytes"],
-            "from_cache": bool(r["from_cache"]),
+            "pull_split": r["pull_split"], "from_cache": bool(r["from_cache"]),
             "tune_s": round(time.perf_counter() - t0, 2),
             "objective_ms_default": round(r["default_ms"], 3), "objective_ms_chosen": round(r["best_ms"], 3)}
 

@@ -108,12 +108,14 @@ def library():
         "gg_graph_set_sssp_delta": ([vp, ctypes.c_float], i32),
         "gg_graph_set_batched_switch": ([vp, u32], i32),
         "gg_graph_set_batched_thread_lanes": ([vp, u32], i32),
+        "gg_graph_set_batched_graph": ([vp, i32], i32),
         "gg_dump_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
         "gg_graph_set_pr_layout": ([vp, i32], i32),
         "gg_graph_set_l1_hot": ([vp, u32], i32),
         "gg_graph_set_dense_push": ([vp, u32], i32),
+        "gg_graph_set_pull_split": ([vp, u32], i32),
         "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
@@ -152,7 +154,7 @@ class _TuneResult(ctypes.Structure):
     _fields_ = [("light_deg", ctypes.c_uint32), ("pull_chunk", ctypes.c_uint32), ("pull_vector", ctypes.c_uint32),
                 ("best_ms", ctypes.c_double),
                 ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32),
-                ("l1_hot_bytes", ctypes.c_uint32)]
+                ("l1_hot_bytes", ctypes.c_uint32), ("pull_split", ctypes.c_uint32)]
 
 
 class RunStats:
@@ -333,6 +335,12 @@ class Graph:
         edges one thread per edge (gg_graph_set_batched_thread_lanes)."""
         _check(library().gg_graph_set_batched_thread_lanes(self.h, int(lanes)))
 
+    def set_batched_graph(self, on):
+        """Batched BFS / SSSP steps device-driven in one CUDA-graph launch per
+        batch (True) or one host wait per step (False, the default;
+        gg_graph_set_batched_graph)."""
+        _check(library().gg_graph_set_batched_graph(self.h, 1 if on else 0))
+
     def set_sssp_delta(self, delta):
         _check(library().gg_graph_set_sssp_delta(self.h, float(delta)))
 
@@ -358,6 +366,11 @@ class Graph:
         """CC / SSSP dense calls with active out-edges below adjacency
         entries / divisor run as a push (0: always pull)."""
         _check(library().gg_graph_set_dense_push(self.h, int(divisor)))
+
+    def set_pull_split(self, light_blocks):
+        """Light-list kernel blocks per SM beside the chunk kernel (1..7), or
+        0 for both over the whole GPU (gg_graph_set_pull_split)."""
+        _check(library().gg_graph_set_pull_split(self.h, int(light_blocks)))
 
     def autotune(self, cache_dir=None, objective=("pagerank", "bfs")):
         """Times the bin candidates on this graph for the named workloads

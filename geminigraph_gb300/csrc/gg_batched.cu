@@ -143,10 +143,20 @@ __device__ __forceinline__ void mark_rows_warp(uint32_t v, u64 m, uint32_t dg, u
 // lane bit takes the first in-neighbour that has it (as bfs.cpp:63-66 does for
 // one root).  next[v] is written for every v (0 for long lists, which the
 // chunk kernel then ORs into).
+// G: a step of the device-driven loop; the step's lanes, masks and
+// iteration come from the pool state st (written by the previous kernel)
+// instead of the arguments.  The same holds for every kernel below with G.
+template <bool G>
 __global__ void __launch_bounds__(256)
     ms_pull_light(Dir d, uint32_t V, u64 alive, const u64 *__restrict__ front, u64 *visit, u64 *next, uint32_t *lvl,
                   uint32_t *par, uint32_t iter, const uint32_t *__restrict__ out_deg, MsCounters *mc,
-                  u64 *lane_sum) {
+                  u64 *lane_sum, const MsState *st) {
+  if (G) {
+    alive = st->active;
+    front = st->front;
+    next = st->next;
+    iter = st->iter;
+  }
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
   LaneSums ls;
@@ -197,9 +207,16 @@ __global__ void __launch_bounds__(256)
 // Long lists: one warp per PULL_CHUNK-edge chunk; a lane bit goes to the
 // entry that wins the atomicOr on next[v] (any in-neighbour in that lane's
 // frontier is a valid parent).  visit[v] is not touched here.
+template <bool G>
 __global__ void __launch_bounds__(256)
     ms_pull_chunks(Dir d, u64 alive, const u64 *__restrict__ front, const u64 *__restrict__ visit, u64 *next,
-                   uint32_t *lvl, uint32_t *par, uint32_t iter) {
+                   uint32_t *lvl, uint32_t *par, uint32_t iter, const MsState *st) {
+  if (G) {
+    alive = st->active;
+    front = st->front;
+    next = st->next;
+    iter = st->iter;
+  }
   const size_t nwarps = (size_t)gridDim.x * 8;
   const unsigned lane = lane_id();
   for (size_t c = (size_t)blockIdx.x * 8 + (threadIdx.x >> 5); c < d.nbigchunks; c += nwarps) {
@@ -228,9 +245,16 @@ __global__ void __launch_bounds__(256)
 
 // The same for a sparse step, over its queue of newly reached vertices: a
 // warp per vertex (thread t: lanes t and t + 32).
+template <bool G>
 __global__ void __launch_bounds__(256)
     ms_mark_levels_q(const uint32_t *__restrict__ q, const unsigned *n_dev, const u64 *__restrict__ next,
-                     uint32_t *lvl, uint32_t iter, const uint32_t *__restrict__ out_deg, u64 *lane_sum) {
+                     uint32_t *lvl, uint32_t iter, const uint32_t *__restrict__ out_deg, u64 *lane_sum,
+                     const MsState *st) {
+  if (G) {
+    q = st->qb;
+    next = st->next;
+    iter = st->iter;
+  }
   __shared__ u64 s_sum[2 * LANES];
   for (int i = threadIdx.x; i < 2 * LANES; i += blockDim.x) s_sum[i] = 0;
   __syncthreads();
@@ -269,8 +293,13 @@ __global__ void __launch_bounds__(256)
 
 
 // visit |= next for the long-list vertices, and their tallies.
+template <bool G>
 __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg,
-                              MsCounters *mc, uint32_t *lvl, uint32_t iter, u64 *lane_sum) {
+                              MsCounters *mc, uint32_t *lvl, uint32_t iter, u64 *lane_sum, const MsState *st) {
+  if (G) {
+    next = st->next;
+    iter = st->iter;
+  }
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
   LaneSums ls;
@@ -298,10 +327,20 @@ __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, c
 // Edge-balanced over the union frontier queue (as push_lb): for edge (u, v)
 // the lanes m = front[u] & ~visit[v] claim v through atomicOr on next[v];
 // the first claimer of v appends it to the touched queue.
+template <bool G>
 __global__ void __launch_bounds__(PUSH_THREADS)
     ms_push(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
             unsigned long long total, Dir d, const u64 *__restrict__ front, const u64 *__restrict__ visit, u64 *next,
-            uint32_t *lvl, uint32_t *par, uint32_t iter, uint32_t *q_out, MsCounters *mc) {
+            uint32_t *lvl, uint32_t *par, uint32_t iter, uint32_t *q_out, MsCounters *mc, const MsState *st) {
+  if (G) {
+    q = st->qa;
+    n = st->nq;
+    total = st->ae;
+    front = st->front;
+    next = st->next;
+    iter = st->iter;
+    q_out = st->qb;
+  }
   __shared__ uint32_t s_lo, s_hi;
   const unsigned long long ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
   for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -339,8 +378,14 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 // After a push: visit |= next over the touched queue, and the tallies.
 // n_dev: the queue length the push kernel counted (read on the device, so
 // the host does not wait between the two kernels).
+template <bool G>
 __global__ void ms_push_finish(const uint32_t *__restrict__ q, const unsigned *n_dev, u64 *visit,
-                               const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg, MsCounters *mc) {
+                               const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg, MsCounters *mc,
+                               const MsState *st) {
+  if (G) {
+    q = st->qb;
+    next = st->next;
+  }
   const uint32_t n = *n_dev;
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
@@ -359,7 +404,13 @@ __global__ void ms_push_finish(const uint32_t *__restrict__ q, const unsigned *n
 }
 
 // Clears mask entries of the n queued vertices.
-__global__ void ms_clear_queue(const uint32_t *__restrict__ q, uint32_t n, u64 *mask) {
+template <bool G>
+__global__ void ms_clear_queue(const uint32_t *__restrict__ q, uint32_t n, u64 *mask, const MsState *st) {
+  if (G) {
+    q = st->qa;
+    n = st->nq;
+    mask = st->front;
+  }
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     mask[q[i]] = 0;
 }
@@ -369,11 +420,43 @@ struct NonzeroMask {
   const u64 *m;
   __device__ __forceinline__ uint32_t operator()(size_t i) const { return m[i] ? 1u : 0u; }
 };
+// The frontier of a device-driven step (the mask array st->front).
+struct NonzeroFront {
+  const MsState *st;
+  __device__ __forceinline__ uint32_t operator()(size_t i) const { return st->front[i] ? 1u : 0u; }
+};
+// G: the frontier is st->front, the queue st->qa, and the queue's length
+// (pos[V]) is recorded in st as a valid queue.
+template <bool G>
 __global__ void ms_compact(const u64 *__restrict__ m, uint32_t V, const uint32_t *__restrict__ pos,
-                           uint32_t *__restrict__ q) {
+                           uint32_t *__restrict__ q, MsState *st) {
+  if (G) {
+    m = st->front;
+    q = st->qa;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->nq = pos[V];
+      st->qvalid = 1;
+    }
+  }
   for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
     if (m[v]) q[pos[v]] = (uint32_t)v;
 }
+
+// next[v] = 0 for every v (a push step after a pull step).
+__global__ void ms_clear_next(const MsState *st, uint32_t V) {
+  u64 *next = st->next;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (size_t)gridDim.x * blockDim.x)
+    next[v] = 0;
+}
+
+// Degree of entry i of the frontier queue of a device-driven step.
+struct QueueDegreeSt {
+  const MsState *st;
+  const uint32_t *deg;
+  __device__ __forceinline__ unsigned long long operator()(size_t i) const {
+    return (unsigned long long)deg[st->qa[i]];
+  }
+};
 
 
 // ---------------------------------------------------------------- pool kernels
@@ -626,10 +709,19 @@ __global__ void __launch_bounds__(256)
 // row of dist[v]).  A lane whose distance at v was lowered gets v's next bit;
 // the first setter of next[v] queues v.  Reads dist[u] as it is now (the
 // fixpoint, hence every lane's result, does not depend on that order).
+template <bool G>
 __global__ void __launch_bounds__(PUSH_THREADS)
     msp_push(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
              unsigned long long total, Dir d, const u64 *__restrict__ front, u64 *next, float *dist, uint32_t *q_out,
-             MsCounters *mc) {
+             MsCounters *mc, const MsState *st) {
+  if (G) {
+    q = st->qa;
+    n = st->nq;
+    total = st->ae;
+    front = st->front;
+    next = st->next;
+    q_out = st->qb;
+  }
   __shared__ unsigned long long s_P[PUSH_STAGE + 1];
   __shared__ unsigned long long s_base[PUSH_STAGE];
   __shared__ uint32_t s_src[PUSH_STAGE];
@@ -703,10 +795,19 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 // The same relaxation, one thread per edge, looping over the SSSP lanes in
 // which the source is on the frontier: for steps with few lanes in flight,
 // where a warp per edge would leave most of its threads idle.
-__global__ void __launch_bounds__(PUSH_THREADS)
+template <bool G>
+__global__ void __launch_bounds__(PUSH_THREADS, 8)
     msp_push_thread(const uint32_t *__restrict__ q, const unsigned long long *__restrict__ P, uint32_t n,
                     unsigned long long total, Dir d, const u64 *__restrict__ front, u64 *next, float *dist,
-                    uint32_t *q_out, MsCounters *mc) {
+                    uint32_t *q_out, MsCounters *mc, const MsState *st) {
+  if (G) {
+    q = st->qa;
+    n = st->nq;
+    total = st->ae;
+    front = st->front;
+    next = st->next;
+    q_out = st->qb;
+  }
   __shared__ unsigned long long s_P[PUSH_STAGE + 1];
   __shared__ unsigned long long s_base[PUSH_STAGE];
   __shared__ uint32_t s_src[PUSH_STAGE];
@@ -779,6 +880,7 @@ size_t LanePool::bytes_needed(const gg_graph *g, Kind kind, bool parents) {
   const size_t V = g->V;
   size_t b = 3 * V * sizeof(u64) + 2 * (V + 1) * sizeof(uint32_t);            // masks, queues
   b += (V + 2) * sizeof(u64) + scan_scratch_elems(V + 1) * sizeof(u64);       // degree prefix + scan
+  b += sizeof(MsState);                                                        // device-driven steps
   b += (bitmap_words32(g->V) + V + 1) * sizeof(uint32_t) + scan_scratch_elems(V) * sizeof(uint32_t);
   if (kind == BFS) b += V * LANES * sizeof(uint32_t) * (parents ? 2 : 1);
   else b += V * LANES * sizeof(float) + V * sizeof(u64);
@@ -809,6 +911,8 @@ int LanePool::open() {
   if (e == cudaSuccess) e = cudaMallocHost(&mc_host_, 512);
   if (e == cudaSuccess) e = cudaMalloc(&out_dev_, 3 * LANES * sizeof(u64));
   if (e == cudaSuccess) e = cudaMallocHost(&out_host_, 3 * LANES * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMalloc(&st_, sizeof(MsState));
+  if (e == cudaSuccess) e = cudaMallocHost(&st_host_, sizeof(MsState));
   if (kind_ == BFS) {
     if (e == cudaSuccess && !parents_) e = cudaMalloc(&lane_sum_, 2 * LANES * sizeof(u64));
     if (e == cudaSuccess) e = cudaMalloc(&visit_, V * sizeof(u64));
@@ -858,12 +962,14 @@ int LanePool::open() {
 
 void LanePool::close() {
   if (s_) cudaStreamSynchronize(s_);
+  destroy_step_graph();
   void *bufs[] = {visit_, front_, next_, lvl_, par_, dist_, q_[0], q_[1], prefix_, scan64_, qpos_, scan32_,
-                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_, pend_, thr_dev_, lane_sum_};
+                  roots_dev_, start_dev_, lanes_dev_, mc_, out_dev_, pend_, thr_dev_, lane_sum_, st_};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (mc_host_) cudaFreeHost(mc_host_);
   if (out_host_) cudaFreeHost(out_host_);
+  if (st_host_) cudaFreeHost(st_host_);
   if (s_) cudaStreamDestroy(s_);
   visit_ = front_ = next_ = nullptr;
   lvl_ = par_ = nullptr;
@@ -877,6 +983,7 @@ void LanePool::close() {
   lanes_dev_ = nullptr;
   mc_ = mc_host_ = nullptr;
   out_dev_ = out_host_ = nullptr;
+  st_ = st_host_ = nullptr;
   s_ = nullptr;
   open_ = false;
 }
@@ -929,12 +1036,22 @@ int LanePool::admit(const uint32_t *roots, const int *lanes, int n) {
   return GG_OK;
 }
 
+template <bool G>
+int LanePool::queue_kernels(int *n) {
+  const uint32_t V = g_->V;
+  if (G)
+    GG_CUDA((exclusive_scan<uint32_t, NonzeroFront>(NonzeroFront{st_}, V, qpos_, scan32_, s_, n)));
+  else
+    GG_CUDA((exclusive_scan<uint32_t, NonzeroMask>(NonzeroMask{front_}, V, qpos_, scan32_, s_, n)));
+  ms_compact<G><<<grid_for(V, 256, g_->num_sms), 256, 0, s_>>>(front_, V, qpos_, q_[cur_], st_);
+  *n += 1;
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 int LanePool::build_queue() {
   const uint32_t V = g_->V;
-  GG_CUDA((exclusive_scan<uint32_t, NonzeroMask>(NonzeroMask{front_}, V, qpos_, scan32_, s_, &launches)));
-  ms_compact<<<grid_for(V, 256, g_->num_sms), 256, 0, s_>>>(front_, V, qpos_, q_[cur_]);
-  launches += 1;
-  GG_CUDA(cudaGetLastError());
+  GG_TRY(queue_kernels<false>(&launches));
   GG_CUDA(cudaMemcpyAsync(mc_host_, qpos_ + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, s_));
   GG_CUDA(cudaStreamSynchronize(s_));
   nq_ = *(uint32_t *)mc_host_;
@@ -948,6 +1065,71 @@ static unsigned push_grid_for(const gg_graph *g, unsigned long long total) {
   return (unsigned)(tiles < 1 ? 1 : (tiles > cap ? cap : tiles));
 }
 
+// Dense BFS step: the light lists, then the long lists' chunks and their finish.
+template <bool G>
+int LanePool::pull_kernels(int *n) {
+  const uint32_t V = g_->V;
+  u64 *ls = par_ ? nullptr : lane_sum_;
+  ms_pull_light<G><<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+      g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_, g_->out.deg, mc_, ls, st_);
+  *n += 1;
+  if (g_->in.nbig) {
+    ms_pull_chunks<G><<<grid_for((size_t)g_->in.nbigchunks * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
+        g_->in, active_, front_, visit_, next_, lvl_, par_, iter_, st_);
+    ms_big_finish<G><<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg,
+                                                                              mc_, lvl_, iter_, ls, st_);
+    *n += 2;
+  }
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// Push over the frontier queue: the prefix of its out-degrees, then the
+// edge-balanced push (BFS), or the warp- or thread-per-edge relaxation (SSSP).
+template <bool G>
+int LanePool::push_kernels(bool per_thread, int *n) {
+  if (G)
+    GG_CUDA((exclusive_scan_dn<unsigned long long, QueueDegreeSt>(QueueDegreeSt{st_, g_->out.deg}, &st_->nq, g_->V,
+                                                                  prefix_, scan64_, s_, n)));
+  else
+    GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
+                                                               scan64_, s_, n)));
+  const unsigned grid = G ? (unsigned)g_->num_sms * 8 : push_grid_for(g_, ae_);
+  if (!G && tr_) GG_TRY(tr_->kbegin());
+  if (kind_ == BFS)
+    ms_push<G><<<grid, PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, visit_, next_, lvl_,
+                                              par_, iter_, q_[cur_ ^ 1], mc_, st_);
+  else
+    (per_thread ? msp_push_thread<G> : msp_push<G>)<<<grid, PUSH_THREADS, 0, s_>>>(
+        q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_, dist_, q_[cur_ ^ 1], mc_, st_);
+  if (!G && tr_) GG_TRY(tr_->kend());
+  *n += 1;
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// After a push: (BFS) visit |= next over the reached queue and its levels;
+// the frontier's masks cleared through its queue.
+template <bool G>
+int LanePool::push_tail(int *n) {
+  // the reached queue's length stays on the device
+  const unsigned *qlen_dev = &mc_->qlen;
+  if (kind_ == BFS) {
+    ms_push_finish<G><<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, visit_, next_, g_->out.deg, mc_, st_);
+    *n += 1;
+  }
+  const unsigned grid = G ? grid_for(g_->V, 256, g_->num_sms) : grid_for(nq_ ? nq_ : 1, 256, g_->num_sms);
+  ms_clear_queue<G><<<grid, 256, 0, s_>>>(q_[cur_], nq_, front_, st_);
+  *n += 1;
+  if (kind_ == BFS && !par_) {
+    ms_mark_levels_q<G><<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, next_, lvl_, iter_, g_->out.deg,
+                                                        lane_sum_, st_);
+    *n += 1;
+  }
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 int LanePool::bfs_step() {
   const uint32_t V = g_->V;
   const bool sparse = ae_ < g_->E / g_->batched_switch_div;
@@ -958,25 +1140,9 @@ int LanePool::bfs_step() {
   if (sparse) {
     if (!qvalid_) GG_TRY(build_queue());
     if (!next_clear_) GG_CUDA(cudaMemsetAsync(next_, 0, sizeof(u64) * V, s_));
-    if (ae_ > 0) {
-      GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
-                                                                 scan64_, s_, &launches)));
-      if (tr_) GG_TRY(tr_->kbegin());
-      ms_push<<<push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, visit_,
-                                                               next_, lvl_, par_, iter_, q_[cur_ ^ 1], mc_);
-      if (tr_) GG_TRY(tr_->kend());
-      launches += 1;
-    }
-    // the queue length stays on the device: one host wait per step
-    const unsigned *qlen_dev = &mc_->qlen;
-    ms_push_finish<<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, visit_, next_, g_->out.deg, mc_);
-    ms_clear_queue<<<grid_for(nq_ ? nq_ : 1, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
-    launches += 2;
-    if (!par_) {
-      ms_mark_levels_q<<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, next_, lvl_, iter_, g_->out.deg,
-                                                       lane_sum_);
-      launches += 1;
-    }
+    if (ae_ > 0) GG_TRY(push_kernels<false>(false, &launches));
+    GG_TRY(push_tail<false>(&launches));
+    // one host wait per step
     GG_TRY(read_counters(&h));
     nq_ = h.qlen;
     qvalid_ = true;
@@ -984,23 +1150,12 @@ int LanePool::bfs_step() {
     next_clear_ = true;
   } else {
     if (tr_) GG_TRY(tr_->kbegin());
-    ms_pull_light<<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-        g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_, g_->out.deg, mc_, par_ ? nullptr : lane_sum_);
-    launches += 1;
-    if (g_->in.nbig) {
-      ms_pull_chunks<<<grid_for((size_t)g_->in.nbigchunks * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-          g_->in, active_, front_, visit_, next_, lvl_, par_, iter_);
-      ms_big_finish<<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_,
-                                                                            lvl_, iter_, par_ ? nullptr : lane_sum_);
-      launches += 2;
-    }
-
+    GG_TRY(pull_kernels<false>(&launches));
     if (tr_) GG_TRY(tr_->kend());
     GG_TRY(read_counters(&h));
     qvalid_ = false;
     next_clear_ = false;
   }
-  GG_CUDA(cudaGetLastError());
   if (tr_) tr_->set_activated(h.touched);
   active_ &= h.alive;
   ae_ = h.edges;
@@ -1016,19 +1171,9 @@ int LanePool::sssp_step() {
   if (!qvalid_) GG_TRY(build_queue());
   GG_CUDA(cudaMemsetAsync(mc_, 0, sizeof(LaneCounters), s_));
   if (!next_clear_) GG_CUDA(cudaMemsetAsync(next_, 0, sizeof(u64) * g_->V, s_));
-  if (ae_ > 0 && nq_ > 0) {
-    GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
-                                                               scan64_, s_, &launches)));
-    if (tr_) GG_TRY(tr_->kbegin());
-    (__builtin_popcountll(active_) <= (int)g_->batched_thread_lanes ? msp_push_thread : msp_push)<<<
-        push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
-                                                              dist_, q_[cur_ ^ 1], mc_);
-    if (tr_) GG_TRY(tr_->kend());
-    launches += 1;
-  }
-  ms_clear_queue<<<grid_for(nq_ ? nq_ : 1, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
-  launches += 1;
-  GG_CUDA(cudaGetLastError());
+  if (ae_ > 0 && nq_ > 0)
+    GG_TRY(push_kernels<false>(__builtin_popcountll(active_) <= (int)g_->batched_thread_lanes, &launches));
+  GG_TRY(push_tail<false>(&launches));
   LaneCounters h;
   GG_TRY(read_counters(&h));
   if (tr_) tr_->set_activated(h.qlen);
@@ -1084,14 +1229,14 @@ int LanePool::sssp_bucket_step() {
     GG_CUDA((exclusive_scan<unsigned long long, QueueDegreeIn>(QueueDegreeIn{q_[cur_], g_->out.deg}, nq_, prefix_,
                                                                scan64_, s_, &launches)));
     if (tr_) GG_TRY(tr_->kbegin());
-    (__builtin_popcountll(active_) <= (int)g_->batched_thread_lanes ? msp_push_thread : msp_push)<<<
+    (__builtin_popcountll(active_) <= (int)g_->batched_thread_lanes ? msp_push_thread<false> : msp_push<false>)<<<
         push_grid_for(g_, ae_), PUSH_THREADS, 0, s_>>>(q_[cur_], prefix_, nq_, ae_, g_->out, front_, next_,
-                                                              dist_, q_[cur_ ^ 1], mc_);
+                                                              dist_, q_[cur_ ^ 1], mc_, nullptr);
     if (tr_) GG_TRY(tr_->kend());
     launches += 1;
   }
   if (nq_) {
-    ms_clear_queue<<<grid_for(nq_, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_);
+    ms_clear_queue<false><<<grid_for(nq_, 256, g_->num_sms), 256, 0, s_>>>(q_[cur_], nq_, front_, nullptr);
     launches += 1;
   }
   GG_CUDA(cudaGetLastError());
@@ -1104,6 +1249,275 @@ int LanePool::step() {
   calls_ += 1;
   if (kind_ == BFS) return bfs_step();
   return bucket_ ? sssp_bucket_step() : sssp_step();
+}
+
+// ---------------------------------------------------------------- device-driven steps
+constexpr uint32_t MS_NO_STEP = 0xffffffffu;
+
+// First kernel of a step of the loop: the step's mode by the rule of
+// bfs_step / sssp_step, from the state the last step left; the step graph's
+// branches switched on or off; the step's counters cleared.
+__global__ void ms_decide(MsState *st, MsCounters *mc, unsigned long long dense_edges, int bfs, uint32_t thread_lanes,
+                          cudaGraphConditionalHandle h_dense, cudaGraphConditionalHandle h_sparse,
+                          cudaGraphConditionalHandle h_build, cudaGraphConditionalHandle h_clear,
+                          cudaGraphConditionalHandle h_push, cudaGraphConditionalHandle h_push_t) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const bool go = st->active != 0 && st->steps < st->cap;
+  const bool dense = go && bfs && st->ae >= dense_edges;
+  const bool sparse = go && !dense;
+  const bool build = sparse && !st->qvalid;
+  const bool clear = sparse && !st->next_clear;
+  const bool push = sparse && st->ae > 0;
+  const bool per_thread = push && !bfs && __popcll(st->active) <= (int)thread_lanes;
+  if (bfs) cudaGraphSetConditional(h_dense, dense);
+  cudaGraphSetConditional(h_sparse, sparse);
+  cudaGraphSetConditional(h_build, build);
+  cudaGraphSetConditional(h_clear, clear);
+  cudaGraphSetConditional(h_push, push && !per_thread);
+  if (!bfs) cudaGraphSetConditional(h_push_t, per_thread);
+  if (!go) {
+    st->mode = MS_NO_STEP;
+    return;
+  }
+  st->mode = (dense ? MS_ROW_DENSE : 0u) | (build ? MS_ROW_BUILD : 0u) | (clear ? MS_ROW_CLEAR : 0u) |
+             (push && !per_thread ? MS_ROW_PUSH : 0u) | (per_thread ? MS_ROW_PUSH_THREAD : 0u);
+  st->iter += 1;
+  mc->alive = 0;
+  mc->edges = 0;
+  mc->touched = 0;
+  mc->qlen = 0;
+}
+
+// Last kernel of a step: its row; the lanes left, the frontier's out-edges
+// and queue; front / next and the two queues swapped; the loop goes on while
+// a lane is active and rows are left.
+__global__ void ms_advance(MsState *st, const MsCounters *mc, int bfs, cudaGraphConditionalHandle h_loop) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t mode = st->mode;
+  if (mode == MS_NO_STEP) {
+    cudaGraphSetConditional(h_loop, 0);
+    return;
+  }
+  const uint32_t r = st->steps;
+  st->row_mode[r] = mode;
+  st->row_ae[r] = st->ae;
+  st->row_reached[r] = bfs ? mc->touched : mc->qlen;
+  st->steps = r + 1;
+  if (mode & MS_ROW_DENSE) {
+    st->qvalid = 0;
+    st->next_clear = 0;
+  } else {
+    // the reached queue is the next frontier's; the push epilogue cleared
+    // the old frontier's masks through its queue
+    st->nq = mc->qlen;
+    st->qvalid = 1;
+    st->next_clear = 1;
+    uint32_t *t = st->qa;
+    st->qa = st->qb;
+    st->qb = t;
+  }
+  st->active &= mc->alive;
+  st->ae = mc->edges;
+  u64 *t = st->front;
+  st->front = st->next;
+  st->next = t;
+  cudaGraphSetConditional(h_loop, st->active != 0 && st->steps < st->cap);
+}
+
+static bool same_dir(const Dir &a, const Dir &b) {
+  return a.light == b.light && a.chunk == b.chunk && a.vec == b.vec && a.off == b.off && a.nbr == b.nbr &&
+         a.w == b.w && a.deg == b.deg && a.nz == b.nz && a.med == b.med && a.nmed == b.nmed && a.heavy == b.heavy &&
+         a.nheavy == b.nheavy && a.heavy_chunk == b.heavy_chunk && a.chunk_owner == b.chunk_owner &&
+         a.nchunks == b.nchunks && a.big == b.big && a.nbig == b.nbig && a.big_chunk == b.big_chunk &&
+         a.big_owner == b.big_owner && a.nbigchunks == b.nbigchunks && a.nv == b.nv && a.ne == b.ne &&
+         a.err == b.err;
+}
+
+bool LanePool::step_graph_current() const {
+  return step_exec_ && same_dir(key_in_, g_->in) && same_dir(key_out_, g_->out) &&
+         key_div_ == g_->batched_switch_div && key_tl_ == g_->batched_thread_lanes;
+}
+
+void LanePool::destroy_step_graph() {
+  if (step_exec_) cudaGraphExecDestroy(step_exec_);
+  if (step_graph_) cudaGraphDestroy(step_graph_);
+  step_exec_ = nullptr;
+  step_graph_ = nullptr;
+}
+
+// The step graph: a loop node whose body is
+//   decide -> [pull] | [push: (queue build) (clear next) -> (push | thread push) -> epilogue] -> advance
+// with every bracket a conditional node that decide switches.  Built once per
+// pool and adjacency (the bins are launch arguments), replayed for every batch.
+int LanePool::build_step_graph() {
+  destroy_step_graph();
+  GG_CUDA(cudaStreamSynchronize(s_));
+  const bool bfs = kind_ == BFS;
+  cudaGraph_t top = nullptr;
+  GG_CUDA(cudaGraphCreate(&top, 0));
+  step_graph_ = top;
+  auto handle = [&](cudaGraphConditionalHandle *h, unsigned dflt, unsigned flags) -> int {
+    GG_CUDA(cudaGraphConditionalHandleCreate(h, top, dflt, flags));
+    return GG_OK;
+  };
+  auto cond = [&](cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, cudaGraphConditionalHandle h,
+                  cudaGraphConditionalNodeType type, cudaGraphNode_t *node, cudaGraph_t *body) -> int {
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = type;
+    np.conditional.size = 1;
+    GG_CUDA(cudaGraphAddNode(node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np));
+    *body = np.conditional.phGraph_out[0];
+    return GG_OK;
+  };
+  // kernels launched by fn, captured into g after deps; sinks: the captured
+  // nodes nothing else depends on
+  auto capture = [&](cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, auto &&fn,
+                     std::vector<cudaGraphNode_t> *sinks) -> int {
+    GG_CUDA(cudaStreamBeginCaptureToGraph(s_, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                          cudaStreamCaptureModeThreadLocal));
+    const int status = fn();
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *d = nullptr;
+    size_t nd = 0;
+    const cudaError_t e = cudaStreamGetCaptureInfo(s_, &cs, nullptr, nullptr, &d, nullptr, &nd);
+    if (e == cudaSuccess && sinks) sinks->assign(d, d + nd);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s_, &captured);
+    if (status != GG_OK) return status;
+    GG_CUDA(e);
+    GG_CUDA(e2);
+    return GG_OK;
+  };
+  cudaGraphConditionalHandle h_loop, h_dense = 0, h_sparse, h_build, h_clear, h_push, h_push_t = 0;
+  GG_TRY(handle(&h_loop, 1, cudaGraphCondAssignDefault));
+  if (bfs) GG_TRY(handle(&h_dense, 0, 0));
+  GG_TRY(handle(&h_sparse, 0, 0));
+  GG_TRY(handle(&h_build, 0, 0));
+  GG_TRY(handle(&h_clear, 0, 0));
+  GG_TRY(handle(&h_push, 0, 0));
+  if (!bfs) GG_TRY(handle(&h_push_t, 0, 0));
+  n_ctl_ = 2;
+  n_dense_ = n_build_ = n_clear_ = n_push_ = n_push_t_ = n_tail_ = 0;
+
+  cudaGraphNode_t loop;
+  cudaGraph_t body;
+  GG_TRY(cond(top, {}, h_loop, cudaGraphCondTypeWhile, &loop, &body));
+  std::vector<cudaGraphNode_t> decided, branches;
+  const unsigned long long dense_edges = g_->E / g_->batched_switch_div;
+  GG_TRY(capture(body, {}, [&]() -> int {
+    ms_decide<<<1, 32, 0, s_>>>(st_, mc_, dense_edges, bfs ? 1 : 0, g_->batched_thread_lanes, h_dense, h_sparse,
+                                h_build, h_clear, h_push, h_push_t);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  }, &decided));
+  cudaGraphNode_t node;
+  cudaGraph_t sub;
+  if (bfs) {
+    GG_TRY(cond(body, decided, h_dense, cudaGraphCondTypeIf, &node, &sub));
+    GG_TRY(capture(sub, {}, [&]() { return pull_kernels<true>(&n_dense_); }, nullptr));
+    branches.push_back(node);
+  }
+  cudaGraph_t sparse;
+  GG_TRY(cond(body, decided, h_sparse, cudaGraphCondTypeIf, &node, &sparse));
+  branches.push_back(node);
+  std::vector<cudaGraphNode_t> ready, pushed;
+  GG_TRY(cond(sparse, {}, h_build, cudaGraphCondTypeIf, &node, &sub));
+  GG_TRY(capture(sub, {}, [&]() { return queue_kernels<true>(&n_build_); }, nullptr));
+  ready.push_back(node);
+  GG_TRY(cond(sparse, {}, h_clear, cudaGraphCondTypeIf, &node, &sub));
+  GG_TRY(capture(sub, {}, [&]() -> int {
+    ms_clear_next<<<grid_for(g_->V, 256, g_->num_sms), 256, 0, s_>>>(st_, g_->V);
+    n_clear_ += 1;
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  }, nullptr));
+  ready.push_back(node);
+  GG_TRY(cond(sparse, ready, h_push, cudaGraphCondTypeIf, &node, &sub));
+  GG_TRY(capture(sub, {}, [&]() { return push_kernels<true>(false, &n_push_); }, nullptr));
+  pushed.push_back(node);
+  if (!bfs) {
+    GG_TRY(cond(sparse, ready, h_push_t, cudaGraphCondTypeIf, &node, &sub));
+    GG_TRY(capture(sub, {}, [&]() { return push_kernels<true>(true, &n_push_t_); }, nullptr));
+    pushed.push_back(node);
+  }
+  GG_TRY(capture(sparse, pushed, [&]() { return push_tail<true>(&n_tail_); }, nullptr));
+  GG_TRY(capture(body, branches, [&]() -> int {
+    ms_advance<<<1, 32, 0, s_>>>(st_, mc_, bfs ? 1 : 0, h_loop);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  }, nullptr));
+  GG_CUDA(cudaGraphInstantiate(&step_exec_, top, 0));
+  key_in_ = g_->in;
+  key_out_ = g_->out;
+  key_div_ = g_->batched_switch_div;
+  key_tl_ = g_->batched_thread_lanes;
+  return GG_OK;
+}
+
+// Runs the step graph until no lane is active: the host state goes to the
+// device before each launch and comes back after it, with one row per step
+// for the trace.  A launch runs at most MS_ROWS steps.
+int LanePool::run_device_steps() {
+  if (!step_graph_current()) GG_TRY(build_step_graph());
+  MsState *h = st_host_;
+  while (active_) {
+    h->front = front_;
+    h->next = next_;
+    h->qa = q_[cur_];
+    h->qb = q_[cur_ ^ 1];
+    h->active = active_;
+    h->ae = ae_;
+    h->nq = nq_;
+    h->iter = iter_;
+    h->qvalid = qvalid_ ? 1u : 0u;
+    h->next_clear = next_clear_ ? 1u : 0u;
+    h->steps = 0;
+    h->cap = MS_ROWS;
+    h->mode = 0;
+    GG_CUDA(cudaMemcpyAsync(st_, h, MS_HEADER, cudaMemcpyHostToDevice, s_));
+    GG_CUDA(cudaGraphLaunch(step_exec_, s_));
+    GG_CUDA(cudaMemcpyAsync(h, st_, sizeof(MsState), cudaMemcpyDeviceToHost, s_));
+    GG_CUDA(cudaStreamSynchronize(s_));
+    const uint32_t steps = h->steps;
+    if (steps == 0 || steps > MS_ROWS) {
+      set_error("device-driven batch ran %u steps", steps);
+      return GG_ERR_CUDA;
+    }
+    for (uint32_t r = 0; r < steps; r++) {
+      const uint32_t m = h->row_mode[r];
+      if (tr_) tr_->add((m & MS_ROW_DENSE) ? 1 : 0, h->row_ae[r], h->row_reached[r]);
+      launches += n_ctl_;
+      if (m & MS_ROW_DENSE) {
+        launches += n_dense_;
+        continue;
+      }
+      if (m & MS_ROW_BUILD) launches += n_build_;
+      if (m & MS_ROW_CLEAR) launches += n_clear_;
+      if (m & MS_ROW_PUSH) launches += n_push_;
+      if (m & MS_ROW_PUSH_THREAD) launches += n_push_t_;
+      launches += n_tail_;
+    }
+    calls_ += (int)steps;
+    front_ = h->front;
+    next_ = h->next;
+    cur_ = h->qa == q_[0] ? 0 : 1;
+    active_ = h->active;
+    ae_ = h->ae;
+    nq_ = h->nq;
+    iter_ = h->iter;
+    qvalid_ = h->qvalid != 0;
+    next_clear_ = h->next_clear != 0;
+  }
+  return GG_OK;
+}
+
+int LanePool::run(bool per_step_timing) {
+  const bool device = g_->batched_graph && !per_step_timing && !(kind_ == SSSP && bucket_);
+  if (device && active_) return run_device_steps();
+  while (active_) GG_TRY(step());
+  return GG_OK;
 }
 
 int LanePool::digest(u64 mask, u64 *reached, u64 *checksum, u64 *edges) {
@@ -1210,7 +1624,7 @@ static int run_batch(gg_graph *g, LanePool::Kind kind, const uint32_t *roots, in
   g->stream = p->stream();  // events and traces on the pool's stream
   status = timed_begin(g);
   if (status == GG_OK) status = p->admit(roots, lanes, nroots);
-  while (status == GG_OK && p->active()) status = p->step();
+  if (status == GG_OK) status = p->run(tr.timing_requested() != 0);
   const u64 mask = nroots == 64 ? ~0ull : ((1ull << nroots) - 1);
   u64 r[LANES], c[LANES], e[LANES];
   if (status == GG_OK) status = p->digest(mask, r, checksum ? c : nullptr, e);
@@ -1289,6 +1703,15 @@ extern "C" int gg_graph_set_batched_thread_lanes(gg_graph *g, uint32_t lanes) {
     return GG_ERR_INVALID;
   }
   g->batched_thread_lanes = lanes;
+  return GG_OK;
+}
+
+extern "C" int gg_graph_set_batched_graph(gg_graph *g, int on) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  g->batched_graph = on ? 1 : 0;
   return GG_OK;
 }
 

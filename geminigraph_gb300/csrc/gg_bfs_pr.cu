@@ -247,6 +247,7 @@ static int pr_run(gg_graph *g, int iterations, T *ranks_host, double *deltas_hos
   key.ranked = ranked;
   key.timing = tr.timing_requested();
   key.hot = hot;
+  key.split = g->pull_light_blocks;
   key.side = g->side;
   const int slot = sizeof(T) == 4 ? 0 : 1;  // one cached graph per precision
   cudaGraphExec_t &exec = g->pr_exec[slot];
@@ -375,6 +376,15 @@ int gg_graph_set_dense_push(gg_graph *g, uint32_t divisor) {
     return GG_ERR_INVALID;
   }
   g->dense_push_div = divisor;
+  return GG_OK;
+}
+
+int gg_graph_set_pull_split(gg_graph *g, uint32_t light_blocks) {
+  if (!g || light_blocks > 7) {
+    set_error("need a graph and 0..7 light blocks per SM");
+    return GG_ERR_INVALID;
+  }
+  g->pull_light_blocks = light_blocks;
   return GG_OK;
 }
 

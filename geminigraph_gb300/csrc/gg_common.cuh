@@ -142,6 +142,7 @@ struct PrGraphKey {
   uint32_t V;
   int32_t iterations, tsize, ranked, timing;
   uint32_t hot;
+  uint32_t split;
   cudaStream_t side;
 };
 
@@ -191,6 +192,14 @@ struct gg_graph {
   // batched SSSP steps with at most this many lanes in flight relax edges
   // one thread per edge (msp_push_thread) instead of one warp per edge
   uint32_t batched_thread_lanes = 16;
+  // batched BFS / SSSP (without buckets) run their steps device-driven: a
+  // CUDA graph whose loop node repeats one step, no host wait between steps
+  // (off by default: measured slower than one host wait per step)
+  int batched_graph = 0;
+  // reduction pulls whose light and chunk kernels run side by side: blocks
+  // per SM of the light kernel (the chunk kernel gets the other 8 - n), so
+  // the two share every SM from the start; 0: each launched over all SMs
+  uint32_t pull_light_blocks = 0;
   int wmin_known = 0;
   float wmin = 0.0f;
   // reduction pulls on the hot-source layout: gathered state of the first

@@ -920,13 +920,19 @@ struct Launch {
       GG_CUDA(cudaEventRecord(g->fork, s));
       GG_CUDA(cudaStreamWaitEvent(g->side, g->fork, 0));
     }
-    pull_light<Op><<<pull_grid(), PULL_THREADS, 0, fork ? g->side : s>>>(d, g->V, op, act, ctr);
+    // split: both kernels resident on every SM at once (8 blocks of 256
+    // threads fill an SM), rather than the chunk kernel waiting for the
+    // light kernel's blocks to retire
+    const uint32_t split = fork && g->pull_light_blocks > 0 && g->pull_light_blocks < 8 ? g->pull_light_blocks : 0;
+    unsigned lg = pull_grid();
+    if (split) lg = grid_for(((size_t)g->V + 31) / 32 * 32, PULL_THREADS, g->num_sms, (int)split);
+    pull_light<Op><<<lg, PULL_THREADS, 0, fork ? g->side : s>>>(d, g->V, op, act, ctr);
     launches += 1;
     if (fork) GG_CUDA(cudaEventRecord(g->join, g->side));
     if (d.nbig) {
       typename Op::Acc *part = nullptr;
       GG_TRY(ws(g, WS_PARTIAL, d.nbigchunks, &part));
-      const unsigned cg = grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, 8);
+      const unsigned cg = grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, split ? 8 - (int)split : 8);
       if (d.vec) {
         if (d.chunk == 128)
           pull_chunks<Op, 4, true><<<cg, PULL_THREADS, 0, s>>>(d, op, part);

@@ -7,6 +7,8 @@
 #ifndef GG_LANES_CUH
 #define GG_LANES_CUH
 
+#include <stddef.h>
+
 #include "gg_common.cuh"
 
 namespace gg {
@@ -25,6 +27,28 @@ struct BucketCounters {
   unsigned int minp[64];      // per lane, the least waiting distance (float bits)
 };
 constexpr size_t BUCKET_OFFSET = 64;
+
+// Device-driven steps: the pool's traversal state in device memory, so that
+// one CUDA-graph launch runs many steps.  A loop node repeats one step's
+// subgraph; its first kernel picks push or pull from the counters of the last
+// step and switches the branches on, its last kernel advances this state and
+// ends the loop when no lane is left (or after `cap` steps, when the host
+// reads the per-step rows and launches again).
+constexpr int MS_ROWS = 1024;
+enum MsRowBits { MS_ROW_DENSE = 1, MS_ROW_BUILD = 2, MS_ROW_CLEAR = 4, MS_ROW_PUSH = 8, MS_ROW_PUSH_THREAD = 16 };
+struct MsState {
+  unsigned long long *front, *next;  // lane masks of this step's frontier / of the lanes it reaches
+  uint32_t *qa, *qb;                 // queue of the frontier / of the vertices this step reaches
+  unsigned long long active;         // lanes still traversing
+  unsigned long long ae;             // out-edges of the union frontier
+  uint32_t nq, iter, qvalid, next_clear;
+  uint32_t steps, cap, mode, pad;    // mode: MsRowBits of the running step
+  // one row per step: mode bits, union frontier out-edges, vertices reached
+  unsigned long long row_ae[MS_ROWS];
+  uint32_t row_mode[MS_ROWS];
+  uint32_t row_reached[MS_ROWS];
+};
+constexpr size_t MS_HEADER = offsetof(MsState, row_ae);
 
 class LanePool {
  public:
@@ -47,6 +71,10 @@ class LanePool {
   int admit(const uint32_t *roots, const int *lanes, int n);
   // One iteration of every active lane; lanes whose frontier empties become done.
   int step();
+  // Steps until no lane is active.  Device-driven (one CUDA-graph launch per
+  // MS_ROWS steps, no host wait between steps) when the graph asks for it
+  // (gg_graph_set_batched_graph) and no per-step kernel time is asked for.
+  int run(bool per_step_timing);
   // Per-lane results of the lanes in mask (arrays indexed by lane):
   // reached vertices, a checksum of the lane's result array (see
   // gg_result_checksum in the header), and the single-root TEPS numerator (BFS).
@@ -63,7 +91,17 @@ class LanePool {
 
  private:
   int read_counters(LaneCounters *h);
+  int run_device_steps();
+  int build_step_graph();
+  void destroy_step_graph();
+  bool step_graph_current() const;
   int build_queue();
+  // the kernels of one step's parts; G: launched into the step graph, their
+  // arguments read from st_ on the device; n counts the launches
+  template <bool G> int queue_kernels(int *n);
+  template <bool G> int pull_kernels(int *n);
+  template <bool G> int push_kernels(bool per_thread, int *n);
+  template <bool G> int push_tail(int *n);
   int bfs_step();
   int sssp_step();
   int sssp_bucket_step();
@@ -103,6 +141,15 @@ class LanePool {
   uint32_t start_[POOL_LANES] = {};
   int calls_ = 0;
   struct Trace *tr_ = nullptr;
+  // device-driven steps
+  MsState *st_ = nullptr, *st_host_ = nullptr;
+  cudaGraph_t step_graph_ = nullptr;
+  cudaGraphExec_t step_exec_ = nullptr;
+  Dir key_in_, key_out_;  // the adjacency (and bins) the step graph was built for
+  uint32_t key_div_ = 0, key_tl_ = 0;
+  // kernel launches of each part of a step (control, pull, queue build,
+  // clear, push, thread push, push epilogue)
+  int n_ctl_ = 0, n_dense_ = 0, n_build_ = 0, n_clear_ = 0, n_push_ = 0, n_push_t_ = 0, n_tail_ = 0;
 };
 
 }  // namespace gg

@@ -55,7 +55,7 @@ static std::string cache_file(const char *dir) {
   } else {
     d = "/tmp/geminigraph_gb300";
   }
-  return d + "/bins_v3.txt";
+  return d + "/bins_v4.txt";
 }
 
 static void mkdirs(const std::string &path) {
@@ -123,14 +123,15 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   const std::string file = cache_file(cache_dir);
   if (FILE *f = fopen(file.c_str(), "r")) {
     char k[160];
-    unsigned light, chunk, vec, l1;
+    unsigned light, chunk, vec, l1, split;
     double ms;
-    while (fscanf(f, "%159s %u %u %u %u %lf", k, &light, &chunk, &vec, &l1, &ms) == 6) {
+    while (fscanf(f, "%159s %u %u %u %u %u %lf", k, &light, &chunk, &vec, &l1, &split, &ms) == 7) {
       if (std::string(k) == key) {
         r.light_deg = light;
         r.pull_chunk = chunk;
         r.pull_vector = vec;
         r.l1_hot_bytes = l1;
+        r.pull_split = split;
         r.best_ms = ms;
         r.from_cache = 1;
       }
@@ -139,6 +140,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     if (r.from_cache) {
       GG_TRY(rebuild_bins(g, r.light_deg, r.pull_chunk, r.pull_vector));
       g->l1_hot_bytes = r.l1_hot_bytes;
+      g->pull_light_blocks = r.pull_split;
       if (out) *out = r;
       return GG_OK;
     }
@@ -224,6 +226,23 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     }
     g->l1_hot_bytes = bh;
   }
+  // the light and chunk kernels of the reduction pulls sharing every SM
+  // (half the blocks each) against each over the whole GPU
+  uint32_t bs = 0;
+  g->pull_light_blocks = 0;
+  if (objective & (GG_TUNE_PAGERANK | GG_TUNE_CC | GG_TUNE_SSSP)) {
+    g->pull_light_blocks = 4;
+    double ms0, ms1;
+    GG_TRY(measure(&ms0));  // warm
+    GG_TRY(measure(&ms1));
+    r.candidates += 1;
+    if (ms1 < best) {
+      best = ms1;
+      bs = 4;
+    }
+    g->pull_light_blocks = bs;
+  }
+  r.pull_split = bs;
   r.l1_hot_bytes = bh;
   r.light_deg = bl;
   r.pull_chunk = bc;
@@ -232,7 +251,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   r.default_ms = def;
   mkdirs(file);
   if (FILE *f = fopen(file.c_str(), "a")) {
-    fprintf(f, "%s %u %u %u %u %.6f\n", key, bl, bc, bv, bh, best);
+    fprintf(f, "%s %u %u %u %u %u %.6f\n", key, bl, bc, bv, bh, bs, best);
     fclose(f);
   }
   if (out) *out = r;

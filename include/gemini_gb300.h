@@ -256,6 +256,20 @@ int gg_graph_set_sssp_delta(gg_graph *g, float delta);
  * is faster at R-MAT 20-26, with 64 the warp form). */
 int gg_graph_set_batched_thread_lanes(gg_graph *g, uint32_t lanes);
 
+/* Batched BFS and SSSP without buckets (gg_bfs_batched, gg_sssp_batched; no
+ * reference counterpart): on, the steps of a batch run device-driven -- one
+ * CUDA-graph launch whose loop node repeats a step, the step's push or pull
+ * picked on the device by the same rule, so the host waits once per batch
+ * (per 1024 steps) instead of once per step.  Off (default): one host wait
+ * per step.  Results and per-step traces do not depend on it.  Measured on
+ * GB300 the host-driven steps are the faster: 64-root batches of R-MAT 24 BFS
+ * 6.79 against 6.86 ms, SSSP 618 against 636 ms, 1024 x 1024 grid BFS 108.5
+ * against 110.4 ms, 8192 x 8192 grid BFS 3.49 against 3.92 s (the step
+ * graph's kernels take their lengths from device memory, so its scans and
+ * pushes launch over the largest grid).  A call that asks for per-call
+ * kernel times (gg_run_stats.call_ms) always runs its steps from the host. */
+int gg_graph_set_batched_graph(gg_graph *g, int on);
+
 /* Batched betweenness centrality (no reference counterpart; per lane the
  * computation of toolkits/bc.cpp:24-196): up to 64 roots in one pass per
  * level.  dependencies and inv_num_paths (either may be NULL) receive
@@ -350,8 +364,10 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
  * 36 candidates (light_deg 16 to 512) on the graph itself with CUDA events, on the workloads the
  * objective mask names (GG_TUNE_PAGERANK: four float PageRank iterations;
  * GG_TUNE_BFS: one BFS; GG_TUNE_BATCHED: one 64-root gg_bfs_batched, and
- * gg_sssp_batched on a weighted graph), keeps the fastest and records it in
- * <cache_dir>/bins_v2.txt (cache_dir NULL: $GG_TUNE_CACHE, else
+ * gg_sssp_batched on a weighted graph; GG_TUNE_SSSP / GG_TUNE_CC: one SSSP /
+ * CC run), keeps the fastest, then times the PageRank L1 policy and (PageRank,
+ * CC, SSSP) the pull split on top of it, and records the result in
+ * <cache_dir>/bins_v4.txt (cache_dir NULL: $GG_TUNE_CACHE, else
  * ~/.cache/geminigraph_gb300) under a fingerprint of the graph and the
  * objective; a later call on the same graph reads the cache instead of
  * searching.  Traversal results (BFS, CC, SSSP) do not depend on the bins;
@@ -366,6 +382,9 @@ typedef struct {
   int32_t from_cache;
   uint32_t l1_hot_bytes; /* the pulls' L1 policy kept (gg_graph_set_l1_hot; PageRank
                             objective: every gather cached, or the hottest 160 KiB) */
+  uint32_t pull_split;   /* the pulls' light kernel blocks per SM beside the chunk kernel
+                            (gg_graph_set_pull_split; PageRank, CC and SSSP objectives:
+                            0, or 4 where it is faster) */
 } gg_tune_result;
 
 int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint32_t pull_vector);
@@ -412,6 +431,15 @@ int gg_graph_set_l1_hot(gg_graph *g, uint32_t l1_bytes);
  * the reference's mode).  Default 4 (measured on R-MAT 25 SSSP: 131 -> 145
  * GTEPS; CC on R-MAT 26 unchanged). */
 int gg_graph_set_dense_push(gg_graph *g, uint32_t divisor);
+
+/* Reduction pulls (PageRank, CC, SSSP, BC backward) whose light-list and
+ * chunk kernels run side by side on two streams (no reference counterpart):
+ * light_blocks in 1..7 launches the light kernel over light_blocks blocks per
+ * SM and the chunk kernel over the other 8 - light_blocks, so both are
+ * resident on every SM from the start; 0 (default) launches each over the
+ * whole GPU, so the chunk kernel's blocks start as the light kernel's retire.
+ * Results do not depend on it. */
+int gg_graph_set_pull_split(gg_graph *g, uint32_t light_blocks);
 
 /* ---- engine primitives ---- */
 

@@ -168,3 +168,77 @@ def test_bfs_batched_switch_point_keeps_levels(case, divisor):
         g.set_batched_switch(0)
     assert np.array_equal(lv, ref[0])
     assert np.array_equal(reached, ref[2])
+
+
+def device_driven(g, fn):
+    """fn() with the batched steps device-driven (one CUDA-graph launch)."""
+    g.set_batched_graph(True)
+    try:
+        return fn()
+    finally:
+        g.set_batched_graph(False)
+
+
+@pytest.mark.parametrize("parents", [False, True])
+def test_bfs_batched_device_driven_equals_host_steps(case, parents):
+    """Device-driven steps (one CUDA-graph launch per batch, push or pull
+    picked on the device) give the levels, per-lane counts and per-step trace
+    of host-driven steps; parents stay valid trees with the same levels."""
+    V, s, d, w, g = case
+    roots = roots_for(V, s, 64, seed=400)
+    dev = device_driven(g, lambda: gg.bfs_batched(g, roots, levels=True, parents=parents))
+    host = gg.bfs_batched(g, roots, levels=True, parents=parents)
+    # asked for per-step kernel times, the steps run from the host
+    timed = device_driven(g, lambda: gg.bfs_batched(g, roots, levels=True, parents=parents, timing=True))
+    for other in (host, timed):
+        assert np.array_equal(dev[0], other[0])
+        assert np.array_equal(dev[2], other[2])
+        assert np.array_equal(dev[3], other[3])
+        assert dev[4].rows() == other[4].rows()
+    if parents:
+        for i, r in enumerate(roots):
+            assert np.array_equal(bfs_levels(dev[1][i], r), dev[0][i])
+    assert dev[4].kernel_launches > 0
+
+
+@pytest.mark.parametrize("thread_lanes", [0, 16, 64])
+def test_sssp_batched_device_driven_equals_host_steps(case, thread_lanes):
+    """The same distances and reached counts for batched SSSP, with each
+    relaxation form (thread per edge up to thread_lanes lanes in flight, warp
+    per edge above)."""
+    V, s, d, w, g = case
+    g.set_batched_thread_lanes(thread_lanes)
+    try:
+        roots = roots_for(V, s, 40, seed=500 + thread_lanes)
+        dev = device_driven(g, lambda: gg.sssp_batched(g, roots))
+        host = gg.sssp_batched(g, roots)
+    finally:
+        g.set_batched_thread_lanes(16)
+    assert np.array_equal(dev[0].view(np.uint32), host[0].view(np.uint32))
+    assert np.array_equal(dev[1], host[1])
+    # a step relaxes from distances as other threads of the same step leave
+    # them, so how many vertices each step lowers varies from run to run (the
+    # fixpoint does not); the first step's row is fixed by the roots
+    assert dev[2].rows()[0] == host[2].rows()[0]
+
+
+def test_batched_device_driven_over_many_launches():
+    """On the 1024 x 1024 grid a corner root is 2,046 levels deep: the
+    device-driven loop runs 1,024 steps per launch, so the batch takes several
+    launches, the state carried between them through the host."""
+    g = gg.Graph.generate(gg.GRID, 1024, 0, 1, weighted=True)
+    try:
+        n = 1024
+        roots = [0, n * n - 1, n * (n // 2) + n // 2, 5]
+        dev = device_driven(g, lambda: gg.bfs_batched(g, roots, levels=True))
+        host = gg.bfs_batched(g, roots, levels=True)
+        assert np.array_equal(dev[0], host[0])
+        assert dev[4].rows() == host[4].rows()
+        assert len(dev[4].rows()) == 2 * (n - 1) + 1 > 1024
+        assert int(dev[0][0].max()) == 2 * (n - 1)
+        ddist = device_driven(g, lambda: gg.sssp_batched(g, roots))
+        hdist = gg.sssp_batched(g, roots)
+        assert np.array_equal(ddist[0].view(np.uint32), hdist[0].view(np.uint32))
+        assert ddist[2].calls > 1024
+    finally:
+        g.close()

@@ -419,6 +419,30 @@ def test_dense_push_matches_oracle(name, div):
         gs.close()
 
 
+@pytest.mark.parametrize("split", [1, 4, 7])
+def test_pull_split_keeps_results(split):
+    """The light and chunk kernels sharing every SM (gg_graph_set_pull_split)
+    change only the launch shapes: PageRank ranks, CC labels and SSSP
+    distances are bit-identical to the unsplit launches', and the oracle's."""
+    V, s, d, w, root = case("rmat16")
+    g = gg.Graph.from_edges(V, s, d, w)
+    gs = gg.Graph.from_edges(V, s, d, symmetric=True)
+    g.set_bins(16, 128, 0)
+    gs.set_bins(16, 128, 0)
+    base = (g.pagerank(8)[0], g.pagerank(8, f32=True)[0], g.sssp(root)[0], gs.cc()[0])
+    g.set_pull_split(split)
+    gs.set_pull_split(split)
+    got = (g.pagerank(8)[0], g.pagerank(8, f32=True)[0], g.sssp(root)[0], gs.cc()[0])
+    for a, b in zip(base, got):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    assert np.array_equal(got[2].view(np.uint32), OracleGraph(V, s, d, w).sssp(root)[0].view(np.uint32))
+    assert np.array_equal(got[3], OracleGraph(V, s, d, symmetric=True).cc()[0])
+    with pytest.raises(gg.GeminiError):
+        g.set_pull_split(8)
+    g.close()
+    gs.close()
+
+
 def test_pagerank_graph_replay():
     """PageRank runs are captured once as a CUDA graph and replayed while
     their arguments are unchanged: replays give bit-identical ranks, per-call
@@ -477,14 +501,16 @@ def test_autotune_picks_and_caches(tmp_path):
     V, s, d, w, root = case("rmat16")
     g = gg.Graph.from_edges(V, s, d, w)
     r1 = g.autotune(str(tmp_path))
-    # 36 bin candidates, then the L1 policy (the default objective includes PageRank)
-    assert r1["candidates"] == 37 and r1["from_cache"] == 0
+    # 36 bin candidates, then the L1 policy and the pull split (the default
+    # objective includes PageRank)
+    assert r1["candidates"] == 38 and r1["from_cache"] == 0
     assert r1["light_deg"] in (16, 32, 64, 128, 256, 512) and r1["pull_chunk"] in (128, 256, 512)
     assert r1["l1_hot_bytes"] in (160 << 10, 0xffffffff)
+    assert r1["pull_split"] in (0, 4)
     assert r1["best_ms"] <= r1["default_ms"]
     g2 = gg.Graph.from_edges(V, s, d, w)
     r2 = g2.autotune(str(tmp_path))
-    key = ("light_deg", "pull_chunk", "pull_vector", "l1_hot_bytes")
+    key = ("light_deg", "pull_chunk", "pull_vector", "l1_hot_bytes", "pull_split")
     assert r2["from_cache"] == 1 and [r2[k] for k in key] == [r1[k] for k in key]
     parent, st = g2.bfs(root)
     assert st.rows() == OracleGraph(V, s, d).bfs(root)[1]
@@ -545,7 +571,7 @@ def test_autotune_objectives(tmp_path):
     seen = set()
     for obj in (("pagerank",), ("bfs",), ("batched",)):
         r = g.autotune(str(tmp_path), objective=obj)
-        assert r["candidates"] == (37 if obj == ("pagerank",) else 36) and r["from_cache"] == 0 and r["best_ms"] > 0
+        assert r["candidates"] == (38 if obj == ("pagerank",) else 36) and r["from_cache"] == 0 and r["best_ms"] > 0
         seen.add(obj)
     assert g.autotune(str(tmp_path), objective=("batched",))["from_cache"] == 1
     lv, _, _, _, _ = gg.bfs_batched(g, [root, 1, 2])

@@ -109,6 +109,7 @@ def library():
         "gg_graph_set_batched_switch": ([vp, u32], i32),
         "gg_graph_set_batched_thread_lanes": ([vp, u32], i32),
         "gg_graph_set_batched_graph": ([vp, i32], i32),
+        "gg_graph_set_batched_lists": ([vp, i32], i32),
         "gg_dump_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_restore_vertex_array": ([vp, u64, u32, ctypes.c_char_p], i32),
         "gg_bc_batched": ([vp, vp, i32, vp, vp, vp, ctypes.POINTER(_Stats)], i32),
@@ -340,6 +341,11 @@ class Graph:
         batch (True) or one host wait per step (False, the default;
         gg_graph_set_batched_graph)."""
         _check(library().gg_graph_set_batched_graph(self.h, 1 if on else 0))
+
+    def set_batched_lists(self, on):
+        """Batched BFS without parents keeps levels as per-step level lists
+        (True, the default) or as per-vertex rows (gg_graph_set_batched_lists)."""
+        _check(library().gg_graph_set_batched_lists(self.h, 1 if on else 0))
 
     def set_sssp_delta(self, delta):
         _check(library().gg_graph_set_sssp_delta(self.h, float(delta)))

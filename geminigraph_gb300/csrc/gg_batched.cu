@@ -88,7 +88,8 @@ __device__ __forceinline__ void ms_record(uint32_t v, u64 bits, uint32_t u, uint
   }
 }
 
-// Levels of newly reached lanes, written a 256-byte row at a time: each lane
+// Levels of newly reached lanes, written a 256-byte row at a time (lvl null:
+// the sums only, the levels going to a level list): each lane
 // of the warp holds a vertex v with its new lanes m and out-degree dg; for
 // every vertex with lanes, thread t writes lvl[v][t] and lvl[v][t + 32] where
 // set and adds them to its per-lane sums (reached, out-degree).
@@ -126,17 +127,45 @@ __device__ __forceinline__ void mark_rows_warp(uint32_t v, u64 m, uint32_t dg, u
     const uint32_t dj = __shfl_sync(GG_FULL, dg, j);
     uint32_t *row = lvl + (size_t)vj * LANES;
     if ((lo >> lane) & 1u) {
-      row[lane] = iter;
+      if (lvl) row[lane] = iter;
       ls.c0 += 1;
       ls.e0 += dj;
     }
     if ((hi >> lane) & 1u) {
-      row[lane + 32] = iter;
+      if (lvl) row[lane + 32] = iter;
       ls.c1 += 1;
       ls.e1 += dj;
     }
   }
 }
+
+// Level-list slots a warp takes from the step's counter at a time (one
+// atomic per LIST_CHUNK entries rather than per warp and vertex group); the
+// slots a warp leaves unused hold empty entries (mask 0).
+constexpr unsigned LIST_CHUNK = 256;
+struct ListCursor {
+  unsigned next = 0, end = 0;  // the warp's slots [next, end), the same in all lanes
+  // Appends (v, iter, m) for the lanes whose m is nonzero.  All lanes call.
+  __device__ __forceinline__ void push(u64 m, uint32_t v, uint32_t iter, LevelEntry *list, unsigned *n) {
+    const unsigned b = __ballot_sync(GG_FULL, m != 0);
+    if (!b) return;
+    const unsigned cnt = __popc(b);
+    if (end - next < cnt) {
+      close(list);
+      unsigned base = 0;
+      if (lane_id() == 0) base = atomicAdd(n, LIST_CHUNK);
+      next = __shfl_sync(GG_FULL, base, 0);
+      end = next + LIST_CHUNK;
+    }
+    if (m) list[next + __popc(b & lanemask_lt())] = make_uint4(v, iter, (unsigned)m, (unsigned)(m >> 32));
+    next += cnt;
+  }
+  // The unused slots as empty entries.  All lanes call.
+  __device__ __forceinline__ void close(LevelEntry *list) {
+    for (unsigned i = next + lane_id(); i < end; i += 32) list[i] = make_uint4(0, 0, 0, 0);
+    next = end;
+  }
+};
 
 // ---------------------------------------------------------------- BFS pull
 // Light lists (<= LIGHT_DEG): the lane's own vertex, in CSC order, so each
@@ -146,11 +175,13 @@ __device__ __forceinline__ void mark_rows_warp(uint32_t v, u64 m, uint32_t dg, u
 // G: a step of the device-driven loop; the step's lanes, masks and
 // iteration come from the pool state st (written by the previous kernel)
 // instead of the arguments.  The same holds for every kernel below with G.
-template <bool G>
+// L: the levels of newly reached lanes go to the level list (list, slots
+// from mc->lpos) instead of the level rows.
+template <bool G, bool L>
 __global__ void __launch_bounds__(256)
     ms_pull_light(Dir d, uint32_t V, u64 alive, const u64 *__restrict__ front, u64 *visit, u64 *next, uint32_t *lvl,
                   uint32_t *par, uint32_t iter, const uint32_t *__restrict__ out_deg, MsCounters *mc,
-                  u64 *lane_sum, const MsState *st) {
+                  u64 *lane_sum, const MsState *st, LevelEntry *list) {
   if (G) {
     alive = st->active;
     front = st->front;
@@ -160,6 +191,7 @@ __global__ void __launch_bounds__(256)
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
   LaneSums ls;
+  ListCursor lc;
   for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < ((size_t)V + 255) / 256 * 256;
        v += (size_t)gridDim.x * blockDim.x) {
     u64 acc = 0;
@@ -198,8 +230,10 @@ __global__ void __launch_bounds__(256)
     }
     // levels of this warp's 32 vertices (without parents; long lists are
     // marked by ms_big_finish)
-    if (lane_sum) mark_rows_warp((uint32_t)v, acc, acc ? out_deg[v] : 0u, lvl, iter, ls);
+    if constexpr (L) lc.push(acc, (uint32_t)v, iter, list, &mc->lpos);
+    if (lane_sum) mark_rows_warp((uint32_t)v, acc, acc ? out_deg[v] : 0u, L ? nullptr : lvl, iter, ls);
   }
+  if (L) lc.close(list);
   ms_flush(mc, t_alive, t_edges, t_touched);
   if (lane_sum) ls.flush(lane_sum);
 }
@@ -268,12 +302,12 @@ __global__ void __launch_bounds__(256)
     const uint32_t dg = out_deg[v];
     uint32_t *row = lvl + (size_t)v * LANES;
     if ((m >> lane) & 1ull) {
-      row[lane] = iter;
+      if (lvl) row[lane] = iter;
       c0 += 1;
       e0 += dg;
     }
     if ((m >> (lane + 32)) & 1ull) {
-      row[lane + 32] = iter;
+      if (lvl) row[lane + 32] = iter;
       c1 += 1;
       e1 += dg;
     }
@@ -293,9 +327,10 @@ __global__ void __launch_bounds__(256)
 
 
 // visit |= next for the long-list vertices, and their tallies.
-template <bool G>
+template <bool G, bool L>
 __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg,
-                              MsCounters *mc, uint32_t *lvl, uint32_t iter, u64 *lane_sum, const MsState *st) {
+                              MsCounters *mc, uint32_t *lvl, uint32_t iter, u64 *lane_sum, const MsState *st,
+                              LevelEntry *list) {
   if (G) {
     next = st->next;
     iter = st->iter;
@@ -303,6 +338,7 @@ __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, c
   u64 t_alive = 0, t_edges = 0;
   unsigned t_touched = 0;
   LaneSums ls;
+  ListCursor lc;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ((size_t)d.nbig + 255) / 256 * 256;
        i += (size_t)gridDim.x * blockDim.x) {
     uint32_t v = 0;
@@ -317,8 +353,10 @@ __global__ void ms_big_finish(Dir d, u64 *visit, const u64 *__restrict__ next, c
         t_touched += 1;
       }
     }
-    if (lane_sum) mark_rows_warp(v, nx, nx ? out_deg[v] : 0u, lvl, iter, ls);
+    if constexpr (L) lc.push(nx, v, iter, list, &mc->lpos);
+    if (lane_sum) mark_rows_warp(v, nx, nx ? out_deg[v] : 0u, L ? nullptr : lvl, iter, ls);
   }
+  if (L) lc.close(list);
   ms_flush(mc, t_alive, t_edges, t_touched);
   if (lane_sum) ls.flush(lane_sum);
 }
@@ -378,10 +416,11 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 // After a push: visit |= next over the touched queue, and the tallies.
 // n_dev: the queue length the push kernel counted (read on the device, so
 // the host does not wait between the two kernels).
+// list: entry i of the level list for queue entry i (iteration iter).
 template <bool G>
 __global__ void ms_push_finish(const uint32_t *__restrict__ q, const unsigned *n_dev, u64 *visit,
                                const u64 *__restrict__ next, const uint32_t *__restrict__ out_deg, MsCounters *mc,
-                               const MsState *st) {
+                               const MsState *st, LevelEntry *list, uint32_t iter) {
   if (G) {
     q = st->qb;
     next = st->next;
@@ -395,6 +434,7 @@ __global__ void ms_push_finish(const uint32_t *__restrict__ q, const unsigned *n
       const uint32_t v = q[i];
       const u64 nx = next[v];
       visit[v] |= nx;
+      if (list) list[i] = make_uint4(v, iter, (unsigned)nx, (unsigned)(nx >> 32));
       t_alive |= nx;
       t_edges += out_deg[v];
       t_touched += 1;
@@ -474,9 +514,10 @@ __global__ void lanes_reset_dist(float *dist, uint32_t V, u64 mask) {
 }
 
 // Roots into lanes: frontier bit, visited bit / distance 0, discovery iteration.
+// list: the roots' level-list entries (instead of their level rows).
 __global__ void lanes_admit(const uint32_t *roots, const int *lanes, int n, u64 *front, u64 *visit, uint32_t *lvl,
                             uint32_t *par, float *dist, uint32_t iter, const uint32_t *out_deg, MsCounters *mc,
-                            u64 *lane_sum) {
+                            u64 *lane_sum, LevelEntry *list) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   u64 edges = 0;
   for (int i = 0; i < n; i++) {
@@ -485,7 +526,12 @@ __global__ void lanes_admit(const uint32_t *roots, const int *lanes, int n, u64 
     if (!front[r]) edges += out_deg[r];
     front[r] |= 1ull << l;
     if (visit) visit[r] |= 1ull << l;
-    if (lvl) lvl[(size_t)r * LANES + l] = iter;
+    if (list) {
+      const u64 m = 1ull << l;
+      list[i] = make_uint4(r, iter, (unsigned)m, (unsigned)(m >> 32));
+    } else if (lvl) {
+      lvl[(size_t)r * LANES + l] = iter;
+    }
     if (par) par[(size_t)r * LANES + l] = r;
     if (dist) dist[(size_t)r * LANES + l] = 0.0f;
     if (lane_sum) {
@@ -494,6 +540,42 @@ __global__ void lanes_admit(const uint32_t *roots, const int *lanes, int n, u64 
     }
   }
   mc->edges = edges;
+}
+
+// Levels of the lanes slot[l] >= 0 from the level lists, lane-major:
+// levels[slot[l] * V + v] = entry iteration - start[l] (the arrays hold -1
+// where a lane did not reach v).
+__global__ void lanes_list_extract(const LevelEntry *__restrict__ list, size_t n, const int *__restrict__ slot,
+                                   const uint32_t *__restrict__ start, uint32_t V, int32_t *levels) {
+  __shared__ int s_slot[LANES];
+  __shared__ uint32_t s_start[LANES];
+  for (int i = threadIdx.x; i < LANES; i += blockDim.x) {
+    s_slot[i] = slot[i];
+    s_start[i] = start[i];
+  }
+  __syncthreads();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const LevelEntry e = list[i];
+    u64 m = ((u64)e.w << 32) | e.z;
+    while (m) {
+      const int l = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      if (s_slot[l] >= 0) levels[(size_t)s_slot[l] * V + e.x] = (int32_t)(e.y - s_start[l]);
+    }
+  }
+}
+
+// The level rows from the level lists (lvl[v][l] = iteration).
+__global__ void lanes_list_rows(const LevelEntry *__restrict__ list, size_t n, uint32_t *lvl) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const LevelEntry e = list[i];
+    u64 m = ((u64)e.w << 32) | e.z;
+    while (m) {
+      const int l = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      lvl[(size_t)e.x * LANES + l] = e.y;
+    }
+  }
 }
 
 // Checksum term of one result entry (matches gg_result_checksum).
@@ -970,6 +1052,10 @@ void LanePool::close() {
   if (mc_host_) cudaFreeHost(mc_host_);
   if (out_host_) cudaFreeHost(out_host_);
   if (st_host_) cudaFreeHost(st_host_);
+  if (list_) cudaFree(list_);
+  list_ = nullptr;
+  list_n_ = list_cap_ = 0;
+  list_mode_ = false;
   if (s_) cudaStreamDestroy(s_);
   visit_ = front_ = next_ = nullptr;
   lvl_ = par_ = nullptr;
@@ -1014,6 +1100,11 @@ int LanePool::admit(const uint32_t *roots, const int *lanes, int n) {
     }
     for (int i = 0; i < n; i++) thr_[lanes[i]] = delta_;
   }
+  if (used_ == 0) {
+    list_mode_ = want_lists_ && kind_ == BFS && !parents_;
+    list_n_ = 0;
+  }
+  if (list_mode_) GG_TRY(list_room((size_t)n));
   const uint32_t V = g_->V;
   GG_CUDA(cudaMemcpyAsync(roots_dev_, roots, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s_));
   GG_CUDA(cudaMemcpyAsync(lanes_dev_, lanes, sizeof(int) * n, cudaMemcpyHostToDevice, s_));
@@ -1024,11 +1115,12 @@ int LanePool::admit(const uint32_t *roots, const int *lanes, int n) {
     lanes_reset_dist<<<grid_for((size_t)V * LANES, 256, g_->num_sms, 16), 256, 0, s_>>>(dist_, V, mask);
   GG_CUDA(cudaMemsetAsync(mc_, 0, sizeof(LaneCounters), s_));
   lanes_admit<<<1, 32, 0, s_>>>(roots_dev_, lanes_dev_, n, front_, visit_, lvl_, par_, dist_, iter_, g_->out.deg, mc_,
-                                lane_sum_);
+                                lane_sum_, list_mode_ ? list_ + list_n_ : nullptr);
   launches += 2;
   GG_CUDA(cudaGetLastError());
   LaneCounters h;
   GG_TRY(read_counters(&h));
+  if (list_mode_) list_n_ += (size_t)n;
   ae_ += h.edges;
   qvalid_ = false;
   used_ |= mask;
@@ -1070,14 +1162,26 @@ template <bool G>
 int LanePool::pull_kernels(int *n) {
   const uint32_t V = g_->V;
   u64 *ls = par_ ? nullptr : lane_sum_;
-  ms_pull_light<G><<<grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
-      g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_, g_->out.deg, mc_, ls, st_);
+  // level lists: entries of this step from list_ + list_n_ (host-driven only)
+  const bool lists = !G && list_mode_;
+  LevelEntry *list = lists ? list_ + list_n_ : nullptr;
+  const unsigned grid = grid_for(((size_t)V + 31) / 32 * 32, 256, g_->num_sms, 8);
+  if (lists)
+    ms_pull_light<G, true><<<grid, 256, 0, s_>>>(g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_,
+                                                g_->out.deg, mc_, ls, st_, list);
+  else
+    ms_pull_light<G, false><<<grid, 256, 0, s_>>>(g_->in, V, active_, front_, visit_, next_, lvl_, par_, iter_,
+                                                 g_->out.deg, mc_, ls, st_, nullptr);
   *n += 1;
   if (g_->in.nbig) {
     ms_pull_chunks<G><<<grid_for((size_t)g_->in.nbigchunks * 32, 256, g_->num_sms, 8), 256, 0, s_>>>(
         g_->in, active_, front_, visit_, next_, lvl_, par_, iter_, st_);
-    ms_big_finish<G><<<grid_for(g_->in.nbig, 256, g_->num_sms), 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg,
-                                                                              mc_, lvl_, iter_, ls, st_);
+    const unsigned fg = grid_for(g_->in.nbig, 256, g_->num_sms);
+    if (lists)
+      ms_big_finish<G, true><<<fg, 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_, lvl_, iter_, ls, st_, list);
+    else
+      ms_big_finish<G, false><<<fg, 256, 0, s_>>>(g_->in, visit_, next_, g_->out.deg, mc_, lvl_, iter_, ls, st_,
+                                                  nullptr);
     *n += 2;
   }
   GG_CUDA(cudaGetLastError());
@@ -1114,15 +1218,18 @@ template <bool G>
 int LanePool::push_tail(int *n) {
   // the reached queue's length stays on the device
   const unsigned *qlen_dev = &mc_->qlen;
+  const bool lists = !G && list_mode_;
   if (kind_ == BFS) {
-    ms_push_finish<G><<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, visit_, next_, g_->out.deg, mc_, st_);
+    ms_push_finish<G><<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, visit_, next_, g_->out.deg, mc_, st_,
+                                                       lists ? list_ + list_n_ : nullptr, iter_);
     *n += 1;
   }
   const unsigned grid = G ? grid_for(g_->V, 256, g_->num_sms) : grid_for(nq_ ? nq_ : 1, 256, g_->num_sms);
   ms_clear_queue<G><<<grid, 256, 0, s_>>>(q_[cur_], nq_, front_, st_);
   *n += 1;
   if (kind_ == BFS && !par_) {
-    ms_mark_levels_q<G><<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, next_, lvl_, iter_, g_->out.deg,
+    ms_mark_levels_q<G><<<g_->num_sms * 4, 256, 0, s_>>>(q_[cur_ ^ 1], qlen_dev, next_, lists ? nullptr : lvl_,
+                                                        iter_, g_->out.deg,
                                                         lane_sum_, st_);
     *n += 1;
   }
@@ -1132,6 +1239,11 @@ int LanePool::push_tail(int *n) {
 
 int LanePool::bfs_step() {
   const uint32_t V = g_->V;
+  // a step appends at most one level-list entry per vertex; a pull step
+  // leaves fewer than 32 empty slots per slot range it takes (ranges hold
+  // LIST_CHUNK) and fewer than LIST_CHUNK at the end of each warp of its two
+  // kernels (at most 64 warps per SM each)
+  if (list_mode_) GG_TRY(list_room(2 * (size_t)V + (size_t)2 * g_->num_sms * 64 * LIST_CHUNK));
   const bool sparse = ae_ < g_->E / g_->batched_switch_div;
   if (tr_) tr_->add(sparse ? 0 : 1, ae_, 0);
   iter_ += 1;
@@ -1157,11 +1269,51 @@ int LanePool::bfs_step() {
     next_clear_ = false;
   }
   if (tr_) tr_->set_activated(h.touched);
+  // every vertex the step reached has one entry (pull: in the slots taken
+  // from mc->lpos, some left empty; push: in the reached queue's order)
+  if (list_mode_) list_n_ += sparse ? h.touched : h.lpos;
   active_ &= h.alive;
   ae_ = h.edges;
   u64 *t = front_;
   front_ = next_;
   next_ = t;
+  return GG_OK;
+}
+
+// Room for `more` level-list entries: the list grows by doubling up to 16
+// entries per vertex (the level rows' 256 bytes); past that the entries so
+// far go into the level rows and the traversals continue on the rows.
+int LanePool::list_room(size_t more) {
+  if (list_n_ + more <= list_cap_) return GG_OK;
+  const size_t V = g_->V;
+  size_t want = list_cap_ ? 2 * list_cap_ : 4 * V + 64;
+  while (want < list_n_ + more) want *= 2;
+  if (want > 16 * V + 64) return lists_to_rows();
+  LevelEntry *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, sizeof(LevelEntry) * want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // out of memory: the rows take over
+    return lists_to_rows();
+  }
+  if (list_n_) GG_CUDA(cudaMemcpyAsync(p, list_, sizeof(LevelEntry) * list_n_, cudaMemcpyDeviceToDevice, s_));
+  GG_CUDA(cudaStreamSynchronize(s_));
+  if (list_) cudaFree(list_);
+  list_ = p;
+  list_cap_ = want;
+  return GG_OK;
+}
+
+// The level lists into the level rows; the running traversals go on with
+// the rows (the per-lane sums are kept by the steps either way).
+int LanePool::lists_to_rows() {
+  if (!list_mode_) return GG_OK;
+  if (list_n_) {
+    lanes_list_rows<<<grid_for(list_n_, 256, g_->num_sms, 8), 256, 0, s_>>>(list_, list_n_, lvl_);
+    launches += 1;
+  }
+  GG_CUDA(cudaGetLastError());
+  list_mode_ = false;
+  list_n_ = 0;
   return GG_OK;
 }
 
@@ -1514,7 +1666,7 @@ int LanePool::run_device_steps() {
 }
 
 int LanePool::run(bool per_step_timing) {
-  const bool device = g_->batched_graph && !per_step_timing && !(kind_ == SSSP && bucket_);
+  const bool device = g_->batched_graph && !per_step_timing && !(kind_ == SSSP && bucket_) && !list_mode_;
   if (device && active_) return run_device_steps();
   while (active_) GG_TRY(step());
   return GG_OK;
@@ -1524,6 +1676,7 @@ int LanePool::digest(u64 mask, u64 *reached, u64 *checksum, u64 *edges) {
   mask &= used_;
   if (!mask) return GG_OK;
   const uint32_t V = g_->V;
+  if (list_mode_ && checksum) GG_TRY(lists_to_rows());
   if (kind_ == BFS && lane_sum_ && !checksum) {
     // the level passes kept the sums: no scan of the graph
     GG_CUDA(cudaMemcpyAsync(out_host_, lane_sum_, 2 * LANES * sizeof(u64), cudaMemcpyDeviceToHost, s_));
@@ -1564,6 +1717,24 @@ int LanePool::extract(u64 mask, int32_t *levels, uint32_t *parents, float *dist)
     if ((mask >> l) & 1ull) lanes[n++] = l;
   if (!n) return GG_OK;
   const uint32_t V = g_->V;
+  if (list_mode_ && kind_ == BFS) {
+    // lane-major levels from the level lists: slot[l] = output row of lane l
+    int slot[LANES];
+    for (int l = 0; l < LANES; l++) slot[l] = -1;
+    for (int j = 0; j < n; j++) slot[lanes[j]] = j;
+    GG_CUDA(cudaMemcpyAsync(lanes_dev_, slot, sizeof(int) * LANES, cudaMemcpyHostToDevice, s_));
+    GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
+    if (levels) {
+      GG_CUDA(cudaMemsetAsync(levels, 0xff, sizeof(int32_t) * (size_t)V * n, s_));
+      if (list_n_)
+        lanes_list_extract<<<grid_for(list_n_, 256, g_->num_sms, 8), 256, 0, s_>>>(list_, list_n_, lanes_dev_,
+                                                                                   start_dev_, V, levels);
+      launches += 1;
+    }
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaStreamSynchronize(s_));
+    return GG_OK;
+  }
   GG_CUDA(cudaMemcpyAsync(lanes_dev_, lanes, sizeof(int) * n, cudaMemcpyHostToDevice, s_));
   GG_CUDA(cudaMemcpyAsync(start_dev_, start_, sizeof(uint32_t) * LANES, cudaMemcpyHostToDevice, s_));
   lanes_extract<<<grid_for(((size_t)V + 31) / 32, 1, g_->num_sms, 16), 256, 0, s_>>>(
@@ -1616,6 +1787,7 @@ static int run_batch(gg_graph *g, LanePool::Kind kind, const uint32_t *roots, in
   if (status != GG_OK) return status;
   Trace tr(stats, g, kind == LanePool::BFS ? "gg_bfs_batched" : "gg_sssp_batched");
   p->set_trace(&tr);
+  p->set_level_lists(kind == LanePool::BFS && !parents && g->batched_lists);
   p->launches = 0;
   const uint32_t V = g->V;
   int lanes[LANES];
@@ -1703,6 +1875,15 @@ extern "C" int gg_graph_set_batched_thread_lanes(gg_graph *g, uint32_t lanes) {
     return GG_ERR_INVALID;
   }
   g->batched_thread_lanes = lanes;
+  return GG_OK;
+}
+
+extern "C" int gg_graph_set_batched_lists(gg_graph *g, int on) {
+  if (!g) {
+    set_error("null graph");
+    return GG_ERR_INVALID;
+  }
+  g->batched_lists = on ? 1 : 0;
   return GG_OK;
 }
 

@@ -196,6 +196,10 @@ struct gg_graph {
   // CUDA graph whose loop node repeats one step, no host wait between steps
   // (off by default: measured slower than one host wait per step)
   int batched_graph = 0;
+  // gg_bfs_batched without parents keeps the lanes' levels as level lists
+  // (one 16-byte entry per vertex and step that reached it) rather than
+  // 256-byte rows per vertex
+  int batched_lists = 1;
   // reduction pulls whose light and chunk kernels run side by side: blocks
   // per SM of the light kernel (the chunk kernel gets the other 8 - n), so
   // the two share every SM from the start; 0: each launched over all SMs

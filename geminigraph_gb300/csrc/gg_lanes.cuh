@@ -20,7 +20,16 @@ struct LaneCounters {
   unsigned long long edges;  // sum of out_degree over the vertices touched this iteration
   unsigned int touched;
   unsigned int qlen;
+  unsigned int lpos;         // level-list entries appended this iteration (pull steps)
+  unsigned int pad;
 };
+
+// Level lists (batched BFS without parents): one 16-byte entry per vertex
+// and iteration in which the vertex gained lanes -- x vertex, y iteration,
+// z / w the low / high half of the lane mask gained.  A lane's level at v is
+// the entry's iteration less the lane's start; the lists hold every lane's
+// levels in place of the 256-byte per-vertex level rows.
+typedef uint4 LevelEntry;
 // Bucketed SSSP filter results, after the LaneCounters in the same buffer.
 struct BucketCounters {
   unsigned long long expand;  // lanes with a vertex below its threshold
@@ -84,6 +93,9 @@ class LanePool {
   // into device buffers (BFS: levels, parents; SSSP: distances in levels_f).
   int extract(unsigned long long mask, int32_t *levels, uint32_t *parents, float *dist);
   void retire(unsigned long long mask) { used_ &= ~mask; }
+  // Level lists instead of level rows for the traversals admitted while the
+  // pool is empty (BFS without parents; takes effect at that admission).
+  void set_level_lists(bool on) { want_lists_ = on; }
   int calls() const { return calls_; }
   bool parents() const { return parents_; }
   void set_trace(struct Trace *tr) { tr_ = tr; }
@@ -92,6 +104,8 @@ class LanePool {
  private:
   int read_counters(LaneCounters *h);
   int run_device_steps();
+  int list_room(size_t more);
+  int lists_to_rows();
   int build_step_graph();
   void destroy_step_graph();
   bool step_graph_current() const;
@@ -141,6 +155,10 @@ class LanePool {
   uint32_t start_[POOL_LANES] = {};
   int calls_ = 0;
   struct Trace *tr_ = nullptr;
+  // level lists: entries in use, capacity, on for the traversals now running
+  LevelEntry *list_ = nullptr;
+  size_t list_n_ = 0, list_cap_ = 0;
+  bool list_mode_ = false, want_lists_ = false;
   // device-driven steps
   MsState *st_ = nullptr, *st_host_ = nullptr;
   cudaGraph_t step_graph_ = nullptr;

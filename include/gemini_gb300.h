@@ -270,6 +270,16 @@ int gg_graph_set_batched_thread_lanes(gg_graph *g, uint32_t lanes);
  * kernel times (gg_run_stats.call_ms) always runs its steps from the host. */
 int gg_graph_set_batched_graph(gg_graph *g, int on);
 
+/* gg_bfs_batched without parents (no reference counterpart): on (default)
+ * the lanes' levels are kept as level lists -- one 16-byte entry (vertex,
+ * step, lanes gained) per vertex and step that reached it, appended by the
+ * step's kernels -- and the per-lane levels, reached counts and TEPS
+ * numerators are read from them; off: as 256-byte rows of 64 levels per
+ * vertex, written as lanes reach it.  A list past 16 entries per vertex
+ * moves into the rows and the batch goes on with rows.  Results do not
+ * depend on it. */
+int gg_graph_set_batched_lists(gg_graph *g, int on);
+
 /* Batched betweenness centrality (no reference counterpart; per lane the
  * computation of toolkits/bc.cpp:24-196): up to 64 roots in one pass per
  * level.  dependencies and inv_num_paths (either may be NULL) receive

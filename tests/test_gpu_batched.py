@@ -242,3 +242,45 @@ def test_batched_device_driven_over_many_launches():
         assert ddist[2].calls > 1024
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("n", [5, 64])
+def test_bfs_batched_level_lists_equal_rows(case, n):
+    """Levels kept as level lists (the default without parents) and as
+    per-vertex rows give the same levels, reached counts, TEPS numerators
+    and per-step trace."""
+    V, s, d, w, g = case
+    roots = roots_for(V, s, max(n, 3), seed=600 + n)[:n]
+    lists = gg.bfs_batched(g, roots, levels=True)
+    g.set_batched_lists(False)
+    try:
+        rows = gg.bfs_batched(g, roots, levels=True)
+    finally:
+        g.set_batched_lists(True)
+    assert np.array_equal(lists[0], rows[0])
+    assert np.array_equal(lists[2], rows[2]) and np.array_equal(lists[3], rows[3])
+    assert lists[4].rows() == rows[4].rows()
+    # without levels asked for, the counts come from the lists alone
+    bare = gg.bfs_batched(g, roots, levels=False)
+    assert np.array_equal(bare[2], rows[2]) and np.array_equal(bare[3], rows[3])
+
+
+def test_bfs_batched_level_lists_move_into_rows():
+    """On a path with 64 roots spread along it, lanes reach most vertices at
+    64 different steps: the level list outgrows 16 entries per vertex, moves
+    into the rows mid-batch, and every lane still has its single-root levels."""
+    V = 4000
+    a = np.arange(V - 1, dtype=np.uint32)
+    s = np.concatenate([a, a + 1])
+    d = np.concatenate([a + 1, a])
+    g = gg.Graph.from_edges(V, s, d)
+    try:
+        roots = [int(x) for x in np.linspace(0, V - 1, 64).astype(np.int64)]
+        lv, _, reached, edges, st = gg.bfs_batched(g, roots, levels=True)
+        for i, r in enumerate(roots):
+            parent, single = g.bfs(r)
+            assert np.array_equal(lv[i], bfs_levels(parent, r)), f"lane {i} root {r}"
+            assert int(reached[i]) == V and int(edges[i]) == single.active_edges_total
+        assert st.calls > 2000
+    finally:
+        g.close()

@@ -1150,8 +1150,7 @@ def main():
     if args.scale is not None:
         WORKLOADS[args.workload] = dict(WORKLOADS[args.workload], scale=args.scale)
         w = WORKLOADS[args.workload]
-        WORKLOADS[args.workload]["desc"] = w["desc"].replace("scale 26", f"scale {args.scale}").replace(
-            "scale 25", f"scale {args.scale}").replace("scale 20", f"scale {args.scale}")
+        WORKLOADS[args.workload]["desc"] = re.sub(r"scale \d+", f"scale {args.scale}", w["desc"])
     dist = Dist()
     try:
         if args.impl == "reference":

@@ -326,7 +326,10 @@ class Graph:
         return self.info()["edges"]
 
     def set_bins(self, light_deg, pull_chunk, pull_vector=1):
-        _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk, 1 if pull_vector else 0))
+        """Pull bins (gg_graph_set_bins): light-list bound, chunk size and the
+        load flags (bit 0: chunk lanes read 16-byte windows; bit 1: light
+        lanes read 32-byte windows)."""
+        _check(library().gg_graph_set_bins(self.h, light_deg, pull_chunk, int(pull_vector)))
 
     def set_batched_switch(self, divisor):
         _check(library().gg_graph_set_batched_switch(self.h, int(divisor)))

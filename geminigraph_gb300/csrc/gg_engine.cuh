@@ -192,7 +192,14 @@ __global__ void __launch_bounds__(PUSH_THREADS)
 //                per vertex combining its chunks
 // The chunk kernel runs beside pull_light (second stream); the finish runs
 // after both and sets its bitmap bits atomically.
-template <class Op>
+// WIN: each lane reads its list by aligned 32-byte windows (two 16-byte
+// loads through L1: eight entries per two load instructions instead of
+// eight), the window's entries of [b, e) gathered together and combined in
+// list order, so the sums equal the scalar form's bit for bit.  The neighbour
+// arrays are padded to a multiple of 64 entries, so a window never leaves
+// the array.  Picked per graph by the autotuner (Dir.vec bit 1).
+constexpr unsigned LIGHT_WIN = 8;
+template <class Op, bool WIN>
 __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op op, ActOut act, Counters *ctr) {
   using Acc = typename Op::Acc;
   Tally t;
@@ -210,16 +217,31 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_light(Dir d, uint32_t V, Op
     uint32_t deg = (uint32_t)(e - b);
     bool a = false;
     if (todo && deg <= d.light) {
-      // four independent gathers in flight, combined in list order
       Acc acc = op.identity(v);
-      unsigned long long k = b;
-      for (; k + 4 <= e; k += 4) {
-        const uint32_t u0 = nbr_at(d, k, GG_SITE), u1 = nbr_at(d, k + 1, GG_SITE), u2 = nbr_at(d, k + 2, GG_SITE), u3 = nbr_at(d, k + 3, GG_SITE);
-        Acc g0 = op.gather(d, k, u0), g1 = op.gather(d, k + 1, u1), g2 = op.gather(d, k + 2, u2),
-            g3 = op.gather(d, k + 3, u3);
-        acc = op.combine(op.combine(op.combine(op.combine(acc, g0), g1), g2), g3);
+      if constexpr (WIN) {
+        for (unsigned long long k = b & ~(unsigned long long)(LIGHT_WIN - 1); k < e; k += LIGHT_WIN) {
+          const uint4 w0 = *reinterpret_cast<const uint4 *>(d.nbr + k);
+          const uint4 w1 = *reinterpret_cast<const uint4 *>(d.nbr + k + 4);
+          const uint32_t u[LIGHT_WIN] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+          Acc gv[LIGHT_WIN];
+#pragma unroll
+          for (unsigned j = 0; j < LIGHT_WIN; j++)
+            gv[j] = k + j >= b && k + j < e ? op.gather(d, k + j, vertex_ok(d, u[j], GG_SITE)) : op.identity_coop();
+#pragma unroll
+          for (unsigned j = 0; j < LIGHT_WIN; j++)
+            if (k + j >= b && k + j < e) acc = op.combine(acc, gv[j]);
+        }
+      } else {
+        // four independent gathers in flight, combined in list order
+        unsigned long long k = b;
+        for (; k + 4 <= e; k += 4) {
+          const uint32_t u0 = nbr_at(d, k, GG_SITE), u1 = nbr_at(d, k + 1, GG_SITE), u2 = nbr_at(d, k + 2, GG_SITE), u3 = nbr_at(d, k + 3, GG_SITE);
+          Acc g0 = op.gather(d, k, u0), g1 = op.gather(d, k + 1, u1), g2 = op.gather(d, k + 2, u2),
+              g3 = op.gather(d, k + 3, u3);
+          acc = op.combine(op.combine(op.combine(op.combine(acc, g0), g1), g2), g3);
+        }
+        for (; k < e; k++) acc = op.combine(acc, op.gather(d, k, nbr_at(d, k, GG_SITE)));
       }
-      for (; k < e; k++) acc = op.combine(acc, op.gather(d, k, nbr_at(d, k, GG_SITE)));
       a = op.finish(v, acc, deg, t);
     }
     if (act.active_out) pull_activate(a, v, g, act, t);
@@ -926,14 +948,17 @@ struct Launch {
     const uint32_t split = fork && g->pull_light_blocks > 0 && g->pull_light_blocks < 8 ? g->pull_light_blocks : 0;
     unsigned lg = pull_grid();
     if (split) lg = grid_for(((size_t)g->V + 31) / 32 * 32, PULL_THREADS, g->num_sms, (int)split);
-    pull_light<Op><<<lg, PULL_THREADS, 0, fork ? g->side : s>>>(d, g->V, op, act, ctr);
+    if (d.vec & 2)
+      pull_light<Op, true><<<lg, PULL_THREADS, 0, fork ? g->side : s>>>(d, g->V, op, act, ctr);
+    else
+      pull_light<Op, false><<<lg, PULL_THREADS, 0, fork ? g->side : s>>>(d, g->V, op, act, ctr);
     launches += 1;
     if (fork) GG_CUDA(cudaEventRecord(g->join, g->side));
     if (d.nbig) {
       typename Op::Acc *part = nullptr;
       GG_TRY(ws(g, WS_PARTIAL, d.nbigchunks, &part));
       const unsigned cg = grid_for((size_t)d.nbigchunks * 32, PULL_THREADS, g->num_sms, split ? 8 - (int)split : 8);
-      if (d.vec) {
+      if (d.vec & 1) {
         if (d.chunk == 128)
           pull_chunks<Op, 4, true><<<cg, PULL_THREADS, 0, s>>>(d, op, part);
         else if (d.chunk == 512)

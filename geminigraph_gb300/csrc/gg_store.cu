@@ -523,8 +523,8 @@ static void free_bins(gg_graph *g, Dir *d) {
 // Rebuilds both directions' degree bins for a light-list bound and a pull
 // chunk size (the autotuner's two knobs).
 int rebuild_bins(gg_graph *g, uint32_t light, uint32_t chunk, uint32_t vec) {
-  if (light < 1 || light > HEAVY_DEG || (chunk != 128 && chunk != 256 && chunk != 512) || vec > 1) {
-    set_error("light list bound must be 1..%u, the pull chunk 128, 256 or 512 and the vector flag 0 or 1",
+  if (light < 1 || light > HEAVY_DEG || (chunk != 128 && chunk != 256 && chunk != 512) || vec > 3) {
+    set_error("light list bound must be 1..%u, the pull chunk 128, 256 or 512 and the vector flags 0..3",
               HEAVY_DEG);
     return GG_ERR_INVALID;
   }

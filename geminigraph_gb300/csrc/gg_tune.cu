@@ -211,6 +211,24 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
         }
       }
   GG_TRY(rebuild_bins(g, bl, bc, bv));
+  // the reduction pulls' light lists read by 32-byte windows (Dir.vec bit
+  // 1), at the chosen bound and, where that wins, at twice it
+  if (objective & (GG_TUNE_PAGERANK | GG_TUNE_CC | GG_TUNE_SSSP)) {
+    const uint32_t tries[2] = {bl, bl * 2 <= HEAVY_DEG ? bl * 2 : 0};
+    for (uint32_t light : tries) {
+      if (!light) break;
+      GG_TRY(rebuild_bins(g, light, bc, bv | 2));
+      double ms0, ms1;
+      GG_TRY(measure(&ms0));  // warm
+      GG_TRY(measure(&ms1));
+      r.candidates += 1;
+      if (!(ms1 < best)) break;
+      best = ms1;
+      bl = light;
+      bv |= 2;
+    }
+    GG_TRY(rebuild_bins(g, bl, bc, bv));
+  }
   uint32_t bh = 0xffffffffu;
   g->l1_hot_bytes = bh;
   if (objective & GG_TUNE_PAGERANK) {

@@ -368,15 +368,19 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
  * core/graph.hpp:1341-1404, balances threads by edge counts at load) ----
  * The pull kernels split vertices into light lists (<= light_deg entries, one
  * lane each) and longer lists cut into pull_chunk-edge warp work items, whose
- * lanes load 16-byte windows of the list (pull_vector = 1) or every 32nd
- * entry (0).  gg_graph_set_bins sets all three (light_deg 1..2048;
- * pull_chunk 128, 256 or 512; pull_vector 0 or 1).  gg_autotune times the
+ * lanes load 16-byte windows of the list (pull_vector bit 0 set) or every
+ * 32nd entry (clear); pull_vector bit 1 makes the reduction pulls' light
+ * lanes read their lists by aligned 32-byte windows (two 16-byte loads per
+ * eight entries) instead of one entry per load.  gg_graph_set_bins sets all
+ * three (light_deg 1..2048; pull_chunk 128, 256 or 512; pull_vector 0..3).  gg_autotune times the
  * 36 candidates (light_deg 16 to 512) on the graph itself with CUDA events, on the workloads the
  * objective mask names (GG_TUNE_PAGERANK: four float PageRank iterations;
  * GG_TUNE_BFS: one BFS; GG_TUNE_BATCHED: one 64-root gg_bfs_batched, and
  * gg_sssp_batched on a weighted graph; GG_TUNE_SSSP / GG_TUNE_CC: one SSSP /
- * CC run), keeps the fastest, then times the PageRank L1 policy and (PageRank,
- * CC, SSSP) the pull split on top of it, and records the result in
+ * CC run), keeps the fastest, then times on top of it (PageRank, CC, SSSP)
+ * the light windows at the chosen bound and, where they win, at twice it,
+ * the PageRank L1 policy and (PageRank, CC, SSSP) the pull split, and records
+ * the result in
  * <cache_dir>/bins_v4.txt (cache_dir NULL: $GG_TUNE_CACHE, else
  * ~/.cache/geminigraph_gb300) under a fingerprint of the graph and the
  * objective; a later call on the same graph reads the cache instead of

@@ -419,6 +419,35 @@ def test_dense_push_matches_oracle(name, div):
         gs.close()
 
 
+@pytest.mark.parametrize("name", ["rmat16", "golden:edgecase", "star"])
+def test_light_windows_keep_results(name):
+    """Light lists read by 32-byte windows (pull_vector bit 1) combine the
+    same entries in the same order: PageRank ranks, CC labels and SSSP
+    distances are bit-identical to the scalar loads', at every light bound;
+    BC dependencies (whose push steps add atomically, in no fixed order)
+    agree within 1e-12."""
+    V, s, d, w, root = case(name)
+    g = gg.Graph.from_edges(V, s, d, w)
+    gs = gg.Graph.from_edges(V, s, d, symmetric=True)
+    for light in (4, 37, 512):
+        got = []
+        for vec in (0, 2, 3, 1):
+            g.set_bins(light, 128, vec)
+            gs.set_bins(light, 128, vec)
+            got.append((g.pagerank(8)[0], g.pagerank(8, f32=True)[0], g.sssp(root)[0], gs.cc()[0], g.bc(root)[0]))
+        for x, y in ((got[0], got[1]), (got[3], got[2])):
+            for a, b in zip(x[:4], y[:4]):
+                assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+            assert np.array_equal(np.isnan(x[4]), np.isnan(y[4]))
+            ok = ~np.isnan(x[4])
+            assert rel_l1(y[4][ok], x[4][ok]) < 1e-12
+    assert np.array_equal(got[1][2].view(np.uint32), OracleGraph(V, s, d, w).sssp(root)[0].view(np.uint32))
+    with pytest.raises(gg.GeminiError):
+        g.set_bins(32, 128, 4)
+    g.close()
+    gs.close()
+
+
 @pytest.mark.parametrize("split", [1, 4, 7])
 def test_pull_split_keeps_results(split):
     """The light and chunk kernels sharing every SM (gg_graph_set_pull_split)
@@ -501,9 +530,9 @@ def test_autotune_picks_and_caches(tmp_path):
     V, s, d, w, root = case("rmat16")
     g = gg.Graph.from_edges(V, s, d, w)
     r1 = g.autotune(str(tmp_path))
-    # 36 bin candidates, then the L1 policy and the pull split (the default
-    # objective includes PageRank)
-    assert r1["candidates"] == 38 and r1["from_cache"] == 0
+    # 36 bin candidates, then the light windows (once or twice), the L1
+    # policy and the pull split (the default objective includes PageRank)
+    assert 39 <= r1["candidates"] <= 40 and r1["from_cache"] == 0
     assert r1["light_deg"] in (16, 32, 64, 128, 256, 512) and r1["pull_chunk"] in (128, 256, 512)
     assert r1["l1_hot_bytes"] in (160 << 10, 0xffffffff)
     assert r1["pull_split"] in (0, 4)
@@ -571,7 +600,8 @@ def test_autotune_objectives(tmp_path):
     seen = set()
     for obj in (("pagerank",), ("bfs",), ("batched",)):
         r = g.autotune(str(tmp_path), objective=obj)
-        assert r["candidates"] == (38 if obj == ("pagerank",) else 36) and r["from_cache"] == 0 and r["best_ms"] > 0
+        assert (39 <= r["candidates"] <= 40 if obj == ("pagerank",) else r["candidates"] == 36)
+        assert r["from_cache"] == 0 and r["best_ms"] > 0
         seen.add(obj)
     assert g.autotune(str(tmp_path), objective=("batched",))["from_cache"] == 1
     lv, _, _, _, _ = gg.bfs_batched(g, [root, 1, 2])

@@ -536,7 +536,9 @@ def tune_bins(g, args):
     if args.bins == "default":
         return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1, "l1_hot_bytes": None,
                 "pull_split": 0}
-    objective = ("pagerank",) if args.workload.startswith("pagerank") else \
+    objective = ("pagerank_f64",) if args.workload == "pagerank_f64" else \
+        ("pagerank",) if args.workload.startswith("pagerank") else \
+        ("bc",) if args.workload == "bc" else \
         ("batched",) if args.workload in ("bfs_batched", "sssp_batched", "bc_batched", "serve") else \
         ("bfs",) if args.workload.startswith("bfs") else ("sssp",) if args.workload == "sssp" else \
         ("cc",) if args.workload == "cc" else ("pagerank", "bfs")

@@ -383,9 +383,9 @@ class Graph:
 
     def autotune(self, cache_dir=None, objective=("pagerank", "bfs")):
         """Times the bin candidates on this graph for the named workloads
-        ("pagerank", "bfs", "batched", "sssp", "cc") and keeps the fastest;
-        cached on disk."""
-        names = {"pagerank": 1, "bfs": 2, "batched": 4, "sssp": 8, "cc": 16}
+        ("pagerank", "pagerank_f64", "bfs", "batched", "sssp", "cc", "bc")
+        and keeps the fastest; cached on disk."""
+        names = {"pagerank": 1, "bfs": 2, "batched": 4, "sssp": 8, "cc": 16, "pagerank_f64": 32, "bc": 64}
         mask = 0
         for o in objective:
             mask |= names[o]

@@ -82,10 +82,14 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     set_error("null graph");
     return GG_ERR_INVALID;
   }
-  const uint32_t all = GG_TUNE_PAGERANK | GG_TUNE_BFS | GG_TUNE_BATCHED | GG_TUNE_SSSP | GG_TUNE_CC;
+  const uint32_t all =
+      GG_TUNE_PAGERANK | GG_TUNE_BFS | GG_TUNE_BATCHED | GG_TUNE_SSSP | GG_TUNE_CC | GG_TUNE_PAGERANK64 | GG_TUNE_BC;
+  // objectives that run reduction pulls (the light windows, L1 policy and
+  // pull split act on those)
+  const uint32_t pulls = GG_TUNE_PAGERANK | GG_TUNE_CC | GG_TUNE_SSSP | GG_TUNE_PAGERANK64 | GG_TUNE_BC;
   if (objective == 0 || (objective & ~all)) {
-    set_error("objective must be a non-empty mask of GG_TUNE_PAGERANK, GG_TUNE_BFS, GG_TUNE_BATCHED, GG_TUNE_SSSP "
-              "and GG_TUNE_CC");
+    set_error("objective must be a non-empty mask of GG_TUNE_PAGERANK, GG_TUNE_BFS, GG_TUNE_BATCHED, GG_TUNE_SSSP, "
+              "GG_TUNE_CC, GG_TUNE_PAGERANK64 and GG_TUNE_BC");
     return GG_ERR_INVALID;
   }
   if (((objective & GG_TUNE_SSSP) && !g->weighted) || ((objective & GG_TUNE_CC) && !g->symmetric)) {
@@ -169,6 +173,14 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
       GG_TRY(gg_pagerank_f32(g, 4, nullptr, nullptr, &st));
       t += st.device_ms;
     }
+    if (objective & GG_TUNE_PAGERANK64) {
+      GG_TRY(gg_pagerank(g, 4, nullptr, nullptr, &st));
+      t += st.device_ms;
+    }
+    if (objective & GG_TUNE_BC) {
+      GG_TRY(gg_bc(g, root, nullptr, nullptr, &st));
+      t += st.device_ms;
+    }
     if (objective & GG_TUNE_BFS) {
       GG_TRY(gg_bfs(g, root, nullptr, &st));
       t += st.device_ms;
@@ -213,7 +225,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   GG_TRY(rebuild_bins(g, bl, bc, bv));
   // the reduction pulls' light lists read by 32-byte windows (Dir.vec bit
   // 1), at the chosen bound and, where that wins, at twice it
-  if (objective & (GG_TUNE_PAGERANK | GG_TUNE_CC | GG_TUNE_SSSP)) {
+  if (objective & pulls) {
     const uint32_t tries[2] = {bl, bl * 2 <= HEAVY_DEG ? bl * 2 : 0};
     for (uint32_t light : tries) {
       if (!light) break;
@@ -231,7 +243,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   }
   uint32_t bh = 0xffffffffu;
   g->l1_hot_bytes = bh;
-  if (objective & GG_TUNE_PAGERANK) {
+  if (objective & (GG_TUNE_PAGERANK | GG_TUNE_PAGERANK64)) {
     const uint32_t hot = 160u << 10;
     g->l1_hot_bytes = hot;
     double ms0, ms1;
@@ -248,7 +260,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   // (half the blocks each) against each over the whole GPU
   uint32_t bs = 0;
   g->pull_light_blocks = 0;
-  if (objective & (GG_TUNE_PAGERANK | GG_TUNE_CC | GG_TUNE_SSSP)) {
+  if (objective & pulls) {
     g->pull_light_blocks = 4;
     double ms0, ms1;
     GG_TRY(measure(&ms0));  // warm

@@ -376,11 +376,12 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
  * 36 candidates (light_deg 16 to 512) on the graph itself with CUDA events, on the workloads the
  * objective mask names (GG_TUNE_PAGERANK: four float PageRank iterations;
  * GG_TUNE_BFS: one BFS; GG_TUNE_BATCHED: one 64-root gg_bfs_batched, and
- * gg_sssp_batched on a weighted graph; GG_TUNE_SSSP / GG_TUNE_CC: one SSSP /
- * CC run), keeps the fastest, then times on top of it (PageRank, CC, SSSP)
- * the light windows at the chosen bound and, where they win, at twice it,
- * the PageRank L1 policy and (PageRank, CC, SSSP) the pull split, and records
- * the result in
+ * gg_sssp_batched on a weighted graph; GG_TUNE_SSSP / GG_TUNE_CC / GG_TUNE_BC:
+ * one SSSP / CC / BC run; GG_TUNE_PAGERANK64: four double PageRank
+ * iterations), keeps the fastest, then times on top of it, for objectives
+ * with reduction pulls (all but BFS and batched), the light windows at the
+ * chosen bound and, where they win, at twice it, the PageRank L1 policy
+ * (PageRank objectives) and the pull split, and records the result in
  * <cache_dir>/bins_v4.txt (cache_dir NULL: $GG_TUNE_CACHE, else
  * ~/.cache/geminigraph_gb300) under a fingerprint of the graph and the
  * objective; a later call on the same graph reads the cache instead of
@@ -408,6 +409,8 @@ int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint
 #define GG_TUNE_BATCHED 4u
 #define GG_TUNE_SSSP 8u    /* one SSSP from the vertex of largest out-degree (weighted graphs) */
 #define GG_TUNE_CC 16u     /* one CC (symmetric graphs) */
+#define GG_TUNE_PAGERANK64 32u /* four double PageRank iterations */
+#define GG_TUNE_BC 64u     /* one BC from the vertex of largest out-degree */
 int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_result *out);
 
 /* PageRank's adjacency layout (no reference counterpart; the reference pulls

@@ -603,6 +603,14 @@ def test_autotune_objectives(tmp_path):
         assert (39 <= r["candidates"] <= 40 if obj == ("pagerank",) else r["candidates"] == 36)
         assert r["from_cache"] == 0 and r["best_ms"] > 0
         seen.add(obj)
+    # double PageRank: windows, L1 policy, split; BC: windows, split
+    r = g.autotune(str(tmp_path), objective=("pagerank_f64",))
+    assert 39 <= r["candidates"] <= 40 and r["best_ms"] > 0
+    r = g.autotune(str(tmp_path), objective=("bc",))
+    assert 38 <= r["candidates"] <= 39 and r["best_ms"] > 0
+    dep, inv, _ = g.bc(root)
+    odep, oinv, _ = OracleGraph(V, s, d, w).bc(root)
+    assert np.array_equal(inv, oinv)
     assert g.autotune(str(tmp_path), objective=("batched",))["from_cache"] == 1
     lv, _, _, _, _ = gg.bfs_batched(g, [root, 1, 2])
     o = OracleGraph(V, s, d, w)

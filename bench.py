@@ -535,7 +535,7 @@ def tune_bins(g, args):
     pick for the workload's kernels (timed on the graph, cached on disk)."""
     if args.bins == "default":
         return {"source": "default", "light_deg": 32, "pull_chunk": 256, "pull_vector": 1, "l1_hot_bytes": None,
-                "pull_split": 0}
+                "pull_split": 0, "bfs_pull": 20}
     objective = ("pagerank_f64",) if args.workload == "pagerank_f64" else \
         ("pagerank",) if args.workload.startswith("pagerank") else \
         ("bc",) if args.workload == "bc" else \
@@ -547,7 +547,7 @@ def tune_bins(g, args):
     return {"source": "autotune(%s)" % "+".join(objective), "light_deg": r["light_deg"],
             "pull_chunk": r["pull_chunk"], "pull_vector": r["pull_vector"],
             "l1_hot_bytes": None if r["l1_hot_bytes"] == 0xffffffff else r["l1_hot_bytes"],
-            "pull_split": r["pull_split"], "from_cache": bool(r["from_cache"]),
+            "pull_split": r["pull_split"], "bfs_pull": r["bfs_pull"], "from_cache": bool(r["from_cache"]),
             "tune_s": round(time.perf_counter() - t0, 2),
             "objective_ms_default": round(r["default_ms"], 3), "objective_ms_chosen": round(r["best_ms"], 3)}
 

@@ -117,6 +117,7 @@ def library():
         "gg_graph_set_l1_hot": ([vp, u32], i32),
         "gg_graph_set_dense_push": ([vp, u32], i32),
         "gg_graph_set_pull_split": ([vp, u32], i32),
+        "gg_graph_set_bfs_pull": ([vp, u32], i32),
         "gg_autotune": ([vp, u32, ctypes.c_char_p, ctypes.POINTER(_TuneResult)], i32),
         "gg_sssp_batched": ([vp, vp, i32, vp, vp, ctypes.POINTER(_Stats)], i32),
     }
@@ -155,7 +156,7 @@ class _TuneResult(ctypes.Structure):
     _fields_ = [("light_deg", ctypes.c_uint32), ("pull_chunk", ctypes.c_uint32), ("pull_vector", ctypes.c_uint32),
                 ("best_ms", ctypes.c_double),
                 ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32),
-                ("l1_hot_bytes", ctypes.c_uint32), ("pull_split", ctypes.c_uint32)]
+                ("l1_hot_bytes", ctypes.c_uint32), ("pull_split", ctypes.c_uint32), ("bfs_pull", ctypes.c_uint32)]
 
 
 class RunStats:
@@ -375,6 +376,11 @@ class Graph:
         """CC / SSSP dense calls with active out-edges below adjacency
         entries / divisor run as a push (0: always pull)."""
         _check(library().gg_graph_set_dense_push(self.h, int(divisor)))
+
+    def set_bfs_pull(self, divisor):
+        """BFS calls pull when active out-edges >= edges / divisor (default
+        20, the reference's switch; gg_graph_set_bfs_pull)."""
+        _check(library().gg_graph_set_bfs_pull(self.h, int(divisor)))
 
     def set_pull_split(self, light_blocks):
         """Light-list kernel blocks per SM beside the chunk kernel (1..7), or

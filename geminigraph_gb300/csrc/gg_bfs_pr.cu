@@ -70,8 +70,12 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
   bool qvalid = true;  // q[cur] holds the active vertices with out-degree > 0
   int cur = 0;
   while (n_act > 0) {
-    bool sparse = ae < g->E / 20;
-    if (sparse && qvalid && Launch::small_ok(nq, ae, md)) {
+    // the reference's mode (core/graph.hpp:1503-1509), recorded in the trace;
+    // the kernel that runs follows g->bfs_pull_div (any in-neighbour on the
+    // frontier is a valid parent, so the levels do not depend on it)
+    const bool sparse = ae < g->E / 20;
+    const bool push = ae < g->E / g->bfs_pull_div;
+    if (sparse && push && qvalid && Launch::small_ok(nq, ae, md)) {
       // consecutive small sparse calls run on the device without host round trips
       GG_TRY((L.small_run<BfsPush, true, uint32_t>(g->out, BfsPush{parent, V, visited}, q, &cur, &nq, &ae, &md, &n_act, visited,
                                                    nullptr, nullptr, nullptr, tr, nullptr)));
@@ -84,17 +88,17 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
     }
     tr.add(sparse ? 0 : 1, ae, 0);
     int nx = cur ^ 1;
-    if (sparse && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[cur], g->out.nz, q[cur], &nq));
+    if (push && ae > 0 && !qvalid) GG_TRY(L.queue_from_bitmap(bm[cur], g->out.nz, q[cur], &nq));
     GG_CUDA(cudaMemsetAsync(bm[nx], 0, words * 4, s));
     GG_TRY(counters_reset(g));
     ActOut a;
     a.active_out = bm[nx];
     a.visited = visited;
-    a.q_out = sparse ? q[nx] : nullptr;
+    a.q_out = push ? q[nx] : nullptr;
     a.qlen = &ctr->qlen;
     a.out_deg = g->out.deg;
     a.queue_nonzero_only = true;
-    if (sparse) {
+    if (push) {
       if (ae > 0) {
         unsigned long long *P;
         GG_TRY(L.scan_queue_degrees(q[cur], nq, g->out.deg, &P));
@@ -114,7 +118,7 @@ static int bfs_run(gg_graph *g, uint32_t root, uint32_t *parent_host, gg_run_sta
     n_act = c.activated;
     nq = c.qlen;
     md = c.maxdeg;
-    qvalid = sparse;
+    qvalid = push;
     ae = c.edges;
     tr.set_activated(c.activated);
     cur = nx;
@@ -376,6 +380,15 @@ int gg_graph_set_dense_push(gg_graph *g, uint32_t divisor) {
     return GG_ERR_INVALID;
   }
   g->dense_push_div = divisor;
+  return GG_OK;
+}
+
+int gg_graph_set_bfs_pull(gg_graph *g, uint32_t divisor) {
+  if (!g || divisor == 0) {
+    set_error("need a graph and a divisor > 0");
+    return GG_ERR_INVALID;
+  }
+  g->bfs_pull_div = divisor;
   return GG_OK;
 }
 

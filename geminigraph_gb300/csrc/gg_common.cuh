@@ -204,6 +204,9 @@ struct gg_graph {
   // per SM of the light kernel (the chunk kernel gets the other 8 - n), so
   // the two share every SM from the start; 0: each launched over all SMs
   uint32_t pull_light_blocks = 0;
+  // gg_bfs calls run the pull kernels when active out-edges >= E / this
+  // (20: the reference's switch; the trace always records the reference's mode)
+  uint32_t bfs_pull_div = 20;
   int wmin_known = 0;
   float wmin = 0.0f;
   // reduction pulls on the hot-source layout: gathered state of the first

@@ -55,7 +55,7 @@ static std::string cache_file(const char *dir) {
   } else {
     d = "/tmp/geminigraph_gb300";
   }
-  return d + "/bins_v4.txt";
+  return d + "/bins_v5.txt";
 }
 
 static void mkdirs(const std::string &path) {
@@ -127,15 +127,16 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   const std::string file = cache_file(cache_dir);
   if (FILE *f = fopen(file.c_str(), "r")) {
     char k[160];
-    unsigned light, chunk, vec, l1, split;
+    unsigned light, chunk, vec, l1, split, bdiv;
     double ms;
-    while (fscanf(f, "%159s %u %u %u %u %u %lf", k, &light, &chunk, &vec, &l1, &split, &ms) == 7) {
+    while (fscanf(f, "%159s %u %u %u %u %u %u %lf", k, &light, &chunk, &vec, &l1, &split, &bdiv, &ms) == 8) {
       if (std::string(k) == key) {
         r.light_deg = light;
         r.pull_chunk = chunk;
         r.pull_vector = vec;
         r.l1_hot_bytes = l1;
         r.pull_split = split;
+        r.bfs_pull = bdiv;
         r.best_ms = ms;
         r.from_cache = 1;
       }
@@ -145,6 +146,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
       GG_TRY(rebuild_bins(g, r.light_deg, r.pull_chunk, r.pull_vector));
       g->l1_hot_bytes = r.l1_hot_bytes;
       g->pull_light_blocks = r.pull_split;
+
       if (out) *out = r;
       return GG_OK;
     }
@@ -273,6 +275,11 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
     g->pull_light_blocks = bs;
   }
   r.pull_split = bs;
+  // the BFS pull divisor is left at the reference's switch: an earlier pull
+  // won on some roots of R-MAT 26 and lost on others, so one timed root
+  // does not choose it
+  const uint32_t bd = g->bfs_pull_div;
+  r.bfs_pull = bd;
   r.l1_hot_bytes = bh;
   r.light_deg = bl;
   r.pull_chunk = bc;
@@ -281,7 +288,7 @@ int gg_autotune(gg_graph *g, uint32_t objective, const char *cache_dir, gg_tune_
   r.default_ms = def;
   mkdirs(file);
   if (FILE *f = fopen(file.c_str(), "a")) {
-    fprintf(f, "%s %u %u %u %u %u %.6f\n", key, bl, bc, bv, bh, bs, best);
+    fprintf(f, "%s %u %u %u %u %u %u %.6f\n", key, bl, bc, bv, bh, bs, bd, best);
     fclose(f);
   }
   if (out) *out = r;

@@ -382,7 +382,7 @@ const void *gg_result_device_ptr(const gg_graph *g, int which);
  * with reduction pulls (all but BFS and batched), the light windows at the
  * chosen bound and, where they win, at twice it, the PageRank L1 policy
  * (PageRank objectives) and the pull split, and records the result in
- * <cache_dir>/bins_v4.txt (cache_dir NULL: $GG_TUNE_CACHE, else
+ * <cache_dir>/bins_v5.txt (cache_dir NULL: $GG_TUNE_CACHE, else
  * ~/.cache/geminigraph_gb300) under a fingerprint of the graph and the
  * objective; a later call on the same graph reads the cache instead of
  * searching.  Traversal results (BFS, CC, SSSP) do not depend on the bins;
@@ -398,8 +398,10 @@ typedef struct {
   uint32_t l1_hot_bytes; /* the pulls' L1 policy kept (gg_graph_set_l1_hot; PageRank
                             objective: every gather cached, or the hottest 160 KiB) */
   uint32_t pull_split;   /* the pulls' light kernel blocks per SM beside the chunk kernel
-                            (gg_graph_set_pull_split; PageRank, CC and SSSP objectives:
+                            (gg_graph_set_pull_split; objectives with reduction pulls:
                             0, or 4 where it is faster) */
+  uint32_t bfs_pull;     /* gg_bfs's pull divisor in effect (gg_graph_set_bfs_pull; not
+                            tuned: an earlier pull wins on some roots and loses on others) */
 } gg_tune_result;
 
 int gg_graph_set_bins(gg_graph *g, uint32_t light_deg, uint32_t pull_chunk, uint32_t pull_vector);
@@ -448,6 +450,14 @@ int gg_graph_set_l1_hot(gg_graph *g, uint32_t l1_bytes);
  * the reference's mode).  Default 4 (measured on R-MAT 25 SSSP: 131 -> 145
  * GTEPS; CC on R-MAT 26 unchanged). */
 int gg_graph_set_dense_push(gg_graph *g, uint32_t divisor);
+
+/* Kernel choice of gg_bfs / gg_bfs_many (the reference's dense mode is the
+ * pull, core/graph.hpp:1503-1509): a call runs the pull kernels when its
+ * active out-edges are at least edges / divisor and the push kernels
+ * otherwise (default 20, the reference's own switch).  Any in-neighbour on
+ * the frontier is a valid parent, so levels, the tree's validity and the
+ * per-call trace (which records the reference's mode) do not depend on it. */
+int gg_graph_set_bfs_pull(gg_graph *g, uint32_t divisor);
 
 /* Reduction pulls (PageRank, CC, SSSP, BC backward) whose light-list and
  * chunk kernels run side by side on two streams (no reference counterpart):

@@ -448,6 +448,28 @@ def test_light_windows_keep_results(name):
     gs.close()
 
 
+@pytest.mark.parametrize("name", ["rmat16", "grid128", "golden:edgecase", "star", "chain"])
+@pytest.mark.parametrize("div", [1, 5, 80, 100000])
+def test_bfs_pull_switch_keeps_levels(name, div):
+    """The BFS kernel switch (pull at active out-edges >= edges / div) moves
+    which kernels run, not the levels, the tree's validity or the recorded
+    per-call trace, which stays the reference's."""
+    V, s, d, w, root = case(name)
+    oparent, otrace = OracleGraph(V, s, d).bfs(root)
+    g = gg.Graph.from_edges(V, s, d)
+    g.set_bfs_pull(div)
+    parent, st = g.bfs(root)
+    assert np.array_equal(bfs_levels(parent, root), bfs_levels(oparent, root))
+    assert st.rows() == otrace
+    ok = parent < V
+    ok[root] = False
+    have = set(zip(s.tolist(), d.tolist()))
+    assert all((int(p), int(v)) in have for v, p in zip(np.nonzero(ok)[0], parent[ok]))
+    with pytest.raises(gg.GeminiError):
+        g.set_bfs_pull(0)
+    g.close()
+
+
 @pytest.mark.parametrize("split", [1, 4, 7])
 def test_pull_split_keeps_results(split):
     """The light and chunk kernels sharing every SM (gg_graph_set_pull_split)
@@ -533,13 +555,14 @@ def test_autotune_picks_and_caches(tmp_path):
     # 36 bin candidates, then the light windows (once or twice), the L1
     # policy and the pull split (the default objective includes PageRank)
     assert 39 <= r1["candidates"] <= 40 and r1["from_cache"] == 0
+    assert r1["bfs_pull"] == 20
     assert r1["light_deg"] in (16, 32, 64, 128, 256, 512) and r1["pull_chunk"] in (128, 256, 512)
     assert r1["l1_hot_bytes"] in (160 << 10, 0xffffffff)
     assert r1["pull_split"] in (0, 4)
     assert r1["best_ms"] <= r1["default_ms"]
     g2 = gg.Graph.from_edges(V, s, d, w)
     r2 = g2.autotune(str(tmp_path))
-    key = ("light_deg", "pull_chunk", "pull_vector", "l1_hot_bytes", "pull_split")
+    key = ("light_deg", "pull_chunk", "pull_vector", "l1_hot_bytes", "pull_split", "bfs_pull")
     assert r2["from_cache"] == 1 and [r2[k] for k in key] == [r1[k] for k in key]
     parent, st = g2.bfs(root)
     assert st.rows() == OracleGraph(V, s, d).bfs(root)[1]

@@ -156,6 +156,30 @@ def test_bfs_batched_64_rmat20_against_oracle():
         assert int(edges[i]) == sum(x[1] for x in otrace)
 
 
+def test_bfs_batched_level_lists_rmat20():
+    """At a million vertices a batch without parents keeps its levels as
+    level lists (the small graphs of test_gpu_batched.py move theirs into
+    rows at the first step): levels, reached counts, TEPS numerators and the
+    per-step trace equal the level rows', and every lane's levels the
+    oracle's."""
+    V, g, og, deg = graph_pair(oracle.RMAT, 20)
+    roots = batch_roots(deg, 3004)
+    lv, pa, reached, edges, st = gg.bfs_batched(g, roots, levels=True, parents=False)
+    assert pa is None
+    g.set_batched_lists(False)
+    try:
+        rl, _, rr, redges, rst = gg.bfs_batched(g, roots, levels=True, parents=False)
+    finally:
+        g.set_batched_lists(True)
+    assert np.array_equal(lv, rl)
+    assert np.array_equal(reached, rr) and np.array_equal(edges, redges)
+    assert st.rows() == rst.rows()
+    outs = pmap(lambda r: og.bfs(r), roots[:16])
+    for i, (r, (oparent, otrace)) in enumerate(zip(roots[:16], outs)):
+        assert np.array_equal(lv[i], oracle.tree_levels(oparent, r)), f"lane {i} root {r}"
+        assert int(edges[i]) == sum(x[1] for x in otrace)
+
+
 def test_sssp_batched_64_rmat20_against_oracle():
     V, g, og, deg = graph_pair(oracle.RMAT, 20, weighted=True)
     roots = batch_roots(deg, 3002)

@@ -43,7 +43,10 @@ graph and kind); build (the partitioned graph build from records in pinned
 host memory under --build-budget-gb, Medges/s, beside the in-core build).
 --adjacency host keeps the neighbour arrays in mapped host memory (read over
 NVLink-C2C) and adds the link rate to the roofline; --bins default skips the
-autotuner.
+autotuner, which otherwise tunes each workload for its own kernels (bins, light
+windows, L1 policy, pull split: config.bins).  The batched BFS keeps its
+levels as level lists during the timed batches (every lane's levels stay on
+the device) and extracts lane-major level arrays in the e2e batches.
 """
 import argparse
 import json
